@@ -1,0 +1,250 @@
+"""Python front end of libactflow (the GB300 solver behind include/actflow.h).
+
+The package is a thin ctypes binding over the C ABI: no computation happens in
+Python.  Importing it loads ``lib/libactflow.so`` (built in-tree by
+``build.py``); if the library is missing the import raises, so a test or
+benchmark can never run on a silent fallback.
+
+    import importlib
+    am = importlib.import_module("2d_active_matter_simulation_gb300")
+    sim = am.Solver(nx=256, ny=256, lx=..., ly=..., dt=..., lam=..., alpha=..., beta=...)
+    sim.set_state(w_hat, mean)          # [ny][nx//2+1] complex, mean[2]
+    energy = sim.step(100)              # energy of the state entering each step
+    w_hat, mean = sim.get_state()
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libactflow.so")
+CLI_PATH = os.path.join(HERE, "lib", "actflow")
+
+AM_OK, AM_ERR_ARG, AM_ERR_CUDA, AM_ERR_NAN, AM_ERR_IO, AM_ERR_SPEC, AM_ERR_OOM, AM_ERR_UNSUPPORTED = range(8)
+FP32, FP64 = 0, 1
+DEALIAS = {"reference": 0, "half": 1, "none": 2}
+FORM_REFERENCE, FORM_GENERAL = 0, 1
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("lx", ctypes.c_double), ("ly", ctypes.c_double), ("dt", ctypes.c_double),
+        ("lam", ctypes.c_double), ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
+        ("gamma0", ctypes.c_double), ("gamma2", ctypes.c_double),
+        ("form", ctypes.c_int), ("dealias", ctypes.c_int), ("precision", ctypes.c_int),
+        ("reserved", ctypes.c_int * 5),
+    ]
+
+
+class Spec(ctypes.Structure):
+    _fields_ = [
+        ("T", ctypes.c_double), ("dt", ctypes.c_double), ("lx", ctypes.c_double), ("ly", ctypes.c_double),
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+        ("lam", ctypes.c_double), ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
+        ("dt_snap", ctypes.c_double), ("gamma0", ctypes.c_double), ("gamma2", ctypes.c_double),
+        ("has_gamma", ctypes.c_int), ("precision", ctypes.c_int), ("dealias", ctypes.c_int),
+        ("initial", ctypes.c_char * 256), ("directory", ctypes.c_char * 1024),
+    ]
+
+
+class ActflowError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(msg)
+        self.status = status
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"libactflow.so not found at {LIB_PATH}: build it first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+    hp = ctypes.c_void_p
+    sig = {
+        "am_create": ([ctypes.POINTER(Params), ctypes.POINTER(hp)], ctypes.c_int),
+        "am_destroy": ([hp], ctypes.c_int),
+        "am_set_stream": ([hp, vp], ctypes.c_int),
+        "am_set_state": ([hp, vp, dp], ctypes.c_int),
+        "am_set_state_real": ([hp, vp, dp, ctypes.c_int], ctypes.c_int),
+        "am_get_state": ([hp, vp, dp], ctypes.c_int),
+        "am_step": ([hp, ctypes.c_int, dp, ip], ctypes.c_int),
+        "am_step_async": ([hp, ctypes.c_int], ctypes.c_int),
+        "am_sync": ([hp], ctypes.c_int),
+        "am_step_profiled": ([hp, ctypes.c_int, dp, dp], ctypes.c_int),
+        "am_launches_per_step": ([hp], ctypes.c_int),
+        "am_device_bytes": ([hp], ctypes.c_longlong),
+        "am_status_string": ([ctypes.c_int], ctypes.c_char_p),
+        "am_last_error": ([hp], ctypes.c_char_p),
+        "am_mask_value": ([ctypes.c_int] * 5, ctypes.c_int),
+        "am_ic_bandlimited": ([ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_double,
+                               ctypes.c_double, ctypes.c_double, dp], ctypes.c_int),
+        "am_spec_read": ([ctypes.c_char_p, ctypes.POINTER(Spec), ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
+        "am_write_snapshot": ([ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, dp], ctypes.c_int),
+        "am_read_snapshot": ([ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, dp], ctypes.c_int),
+        "am_append_energy": ([ctypes.c_char_p, ctypes.c_longlong, ctypes.c_int, ctypes.c_float, dp,
+                              ctypes.c_int], ctypes.c_int),
+        "am_cli_main": ([ctypes.c_int, ctypes.POINTER(ctypes.c_char_p)], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    return L
+
+
+lib = _load()
+
+# Every symbol include/actflow.h declares (checked by the CPU test suite).
+EXPORTED = [
+    "am_create", "am_destroy", "am_set_stream", "am_set_state", "am_set_state_real", "am_get_state",
+    "am_step", "am_step_async", "am_sync", "am_step_profiled", "am_launches_per_step", "am_device_bytes", "am_status_string",
+    "am_last_error", "am_mask_value", "am_ic_bandlimited", "am_spec_read", "am_write_snapshot",
+    "am_read_snapshot", "am_append_energy", "am_cli_main",
+]
+
+
+def status_string(s):
+    return lib.am_status_string(s).decode()
+
+
+def _check(st, h=None, what=""):
+    if st != AM_OK:
+        detail = lib.am_last_error(h).decode() if h else ""
+        raise ActflowError(st, f"{what}: {status_string(st)} {detail}".strip())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Solver:
+    """One simulation on the GPU (an am_handle)."""
+
+    def __init__(self, nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None,
+                 dealias="reference", precision="fp32"):
+        form = FORM_REFERENCE if gamma0 is None else FORM_GENERAL
+        self.precision = FP64 if precision in ("fp64", FP64) else FP32
+        self.params = Params(nx, ny, lx, ly, dt, lam, alpha, beta,
+                             0.0 if gamma0 is None else gamma0, 0.0 if gamma2 is None else gamma2,
+                             form, DEALIAS[dealias] if isinstance(dealias, str) else int(dealias),
+                             self.precision)
+        self.nx, self.ny = nx, ny
+        self.h = ctypes.c_void_p()
+        _check(lib.am_create(ctypes.byref(self.params), ctypes.byref(self.h)), None, "am_create")
+        self.cdtype = np.complex128 if self.precision == FP64 else np.complex64
+        self.rdtype = np.float64 if self.precision == FP64 else np.float32
+
+    def close(self):
+        if self.h:
+            lib.am_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        _check(lib.am_set_stream(self.h, ctypes.c_void_p(stream_ptr)), self.h, "am_set_stream")
+
+    def set_state(self, w_hat, mean=(0.0, 0.0)):
+        w = np.ascontiguousarray(w_hat, dtype=self.cdtype)
+        assert w.shape == (self.ny, self.nx // 2 + 1)
+        m = np.array(mean, dtype=np.float64)
+        _check(lib.am_set_state(self.h, w.ctypes.data, _dptr(m)), self.h, "am_set_state")
+
+    def set_state_real(self, w_real, mean=(0.0, 0.0), mask_and_zero_mean=True):
+        w = np.ascontiguousarray(w_real, dtype=self.rdtype)
+        assert w.shape == (self.ny, self.nx)
+        m = np.array(mean, dtype=np.float64)
+        _check(lib.am_set_state_real(self.h, w.ctypes.data, _dptr(m), int(mask_and_zero_mean)), self.h,
+               "am_set_state_real")
+
+    def get_state(self):
+        w = np.zeros((self.ny, self.nx // 2 + 1), dtype=self.cdtype)
+        m = np.zeros(2, dtype=np.float64)
+        _check(lib.am_get_state(self.h, w.ctypes.data, _dptr(m)), self.h, "am_get_state")
+        return w, m
+
+    def step(self, nsteps, energy=True):
+        e = np.zeros(max(nsteps, 1), dtype=np.float64)
+        nan_at = ctypes.c_int(-1)
+        st = lib.am_step(self.h, nsteps, _dptr(e) if energy else None, ctypes.byref(nan_at))
+        if st == AM_ERR_NAN:
+            raise ActflowError(st, f"NaN after step {nan_at.value}")
+        _check(st, self.h, "am_step")
+        return e[:nsteps]
+
+    def step_async(self, nsteps):
+        _check(lib.am_step_async(self.h, nsteps), self.h, "am_step_async")
+
+    def sync(self):
+        _check(lib.am_sync(self.h), self.h, "am_sync")
+
+    def step_profiled(self, nsteps):
+        """Per-kernel CUDA-event times (ms) summed over nsteps: (row[4], col[4])."""
+        r = np.zeros(4)
+        c = np.zeros(4)
+        _check(lib.am_step_profiled(self.h, nsteps, _dptr(r), _dptr(c)), self.h, "am_step_profiled")
+        return r, c
+
+    @property
+    def launches_per_step(self):
+        return lib.am_launches_per_step(self.h)
+
+    @property
+    def device_bytes(self):
+        return lib.am_device_bytes(self.h)
+
+
+def mask_value(nx, ny, dealias, ix, iy):
+    return lib.am_mask_value(nx, ny, DEALIAS[dealias] if isinstance(dealias, str) else int(dealias), ix, iy)
+
+
+def ic_bandlimited(nx, ny, seed, kmin=1.0, kmax=8.0, rms=0.01):
+    w = np.zeros((ny, nx // 2 + 1), dtype=np.complex128)
+    _check(lib.am_ic_bandlimited(nx, ny, seed, kmin, kmax, rms, w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+           None, "am_ic_bandlimited")
+    return w
+
+
+def read_spec(directory):
+    s = Spec()
+    err = ctypes.create_string_buffer(1024)
+    st = lib.am_spec_read(directory.encode(), ctypes.byref(s), err, 1024)
+    if st != AM_OK:
+        raise ActflowError(st, err.value.decode())
+    return s
+
+
+def write_snapshot(path, w_hat, mean, precision="fp32"):
+    prec = FP64 if precision in ("fp64", FP64) else FP32
+    w = np.ascontiguousarray(w_hat, dtype=np.complex128 if prec == FP64 else np.complex64)
+    ny, nxh = w.shape
+    m = np.array(mean, dtype=np.float64)
+    _check(lib.am_write_snapshot(path.encode(), 2 * (nxh - 1), ny, prec, w.ctypes.data, _dptr(m)), None,
+           "am_write_snapshot")
+
+
+def read_snapshot(path, nx, ny, precision="fp32"):
+    prec = FP64 if precision in ("fp64", FP64) else FP32
+    w = np.zeros((ny, nx // 2 + 1), dtype=np.complex128 if prec == FP64 else np.complex64)
+    m = np.zeros(2, dtype=np.float64)
+    _check(lib.am_read_snapshot(path.encode(), nx, ny, prec, w.ctypes.data, _dptr(m)), None, "am_read_snapshot")
+    return w, m
+
+
+def append_energy(path, m0, dt, energy, precision="fp32"):
+    prec = FP64 if precision in ("fp64", FP64) else FP32
+    e = np.ascontiguousarray(energy, dtype=np.float64)
+    _check(lib.am_append_energy(path.encode(), m0, len(e), dt, _dptr(e), prec), None, "am_append_energy")
+
+
+def cli_main(args):
+    """Run the drop-in program in-process: cli_main(["actflow", dir])."""
+    argv = (ctypes.c_char_p * len(args))(*[a.encode() for a in args])
+    return lib.am_cli_main(len(args), argv)

@@ -1,0 +1,540 @@
+// C ABI of the actflow solver (declared in include/actflow.h).
+//
+// One handle = one simulation on one GPU stream.  Device memory per handle
+// (complex half-plane fields in the tiled layout, s = sizeof(cpx<T>)):
+//   u0, acc            spectral state w_old / w_new                2 fields
+//   fa, fx, fy         next stage input a, ux, uy in (kx, y)        3 fields
+//   P, Q               real-space products after R2C along x        2 fields
+//   stage              host <-> device staging in the reference layout
+// plus per-row sums, scalars, the energy ring and small tables.  A step is 8
+// kernel launches (row pass + column pass per RK stage), captured once into a
+// CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/actflow.h"
+#include "host_tables.h"
+#include "kernels.h"
+
+using namespace af;
+
+namespace {
+
+constexpr int ECAP = 4096;   // energy ring entries per handle
+
+bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+int ilog2(int n)
+{
+    int l = 0;
+    while ((1 << l) < n) l++;
+    return l;
+}
+
+}  // namespace
+
+struct am_handle {
+    am_params p{};
+    int nxh = 0, nt = 0, W = 0, lognx = 0, logny = 0;
+    bool fp64 = false;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+    // device memory
+    void *u0 = nullptr, *acc = nullptr, *fa = nullptr, *fx = nullptr, *fy = nullptr, *P = nullptr, *Q = nullptr;
+    void *stage = nullptr, *twx = nullptr, *twy = nullptr, *kxt = nullptr, *kyt = nullptr;
+    double *rowp = nullptr, *energy = nullptr;
+    Scalars *sc = nullptr;
+    long long bytes = 0;
+    // graph of one step
+    cudaGraphExec_t graph = nullptr;
+    bool state_loaded = false;
+    std::string err;
+    // kernel arguments (scalar part filled at create)
+    StepArgs<float> a32{};
+    StepArgs<double> a64{};
+};
+
+static am_status cuda_fail(am_handle *h, cudaError_t e, const char *what)
+{
+    if (h) {
+        h->err = std::string(what) + ": " + cudaGetErrorString(e);
+    }
+    return e == cudaErrorMemoryAllocation ? AM_ERR_OOM : AM_ERR_CUDA;
+}
+
+#define CK(h, call)                                            \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+    } while (0)
+
+template <typename T>
+static StepArgs<T> &args_of(am_handle *h);
+template <>
+StepArgs<float> &args_of<float>(am_handle *h) { return h->a32; }
+template <>
+StepArgs<double> &args_of<double>(am_handle *h) { return h->a64; }
+
+template <typename T>
+static const KernelTable<T> &table();
+template <>
+const KernelTable<float> &table<float>() { return kernels_f32(); }
+template <>
+const KernelTable<double> &table<double>() { return kernels_f64(); }
+
+template <typename T>
+static am_status alloc_and_tables(am_handle *h)
+{
+    const am_params &p = h->p;
+    const int nx = p.nx, ny = p.ny;
+    const int W = Tile<T>::W;
+    h->W = W;
+    h->nxh = nx / 2 + 1;
+    h->nt = (h->nxh + W - 1) / W;
+    const size_t field = (size_t)h->nt * W * ny * sizeof(cpx<T>);
+    const size_t stage = (size_t)ny * h->nxh * sizeof(cpx<T>);
+    void **fields[] = {&h->u0, &h->acc, &h->fa, &h->fx, &h->fy, &h->P, &h->Q};
+    for (void **f : fields) {
+        CK(h, cudaMalloc(f, field));
+        CK(h, cudaMemsetAsync(*f, 0, field, h->stream));
+        h->bytes += field;
+    }
+    CK(h, cudaMalloc(&h->stage, stage));
+    h->bytes += stage;
+    CK(h, cudaMalloc(&h->twx, nx * sizeof(cpx<T>)));
+    CK(h, cudaMalloc(&h->twy, ny * sizeof(cpx<T>)));
+    CK(h, cudaMalloc(&h->kxt, h->nt * W * sizeof(T)));
+    CK(h, cudaMalloc(&h->kyt, ny * sizeof(T)));
+    CK(h, cudaMalloc(&h->rowp, (size_t)ny * 3 * sizeof(double)));
+    CK(h, cudaMemsetAsync(h->rowp, 0, (size_t)ny * 3 * sizeof(double), h->stream));
+    CK(h, cudaMalloc(&h->energy, ECAP * sizeof(double)));
+    CK(h, cudaMalloc(&h->sc, sizeof(Scalars)));
+    h->bytes += nx * sizeof(cpx<T>) + ny * sizeof(cpx<T>) + h->nt * W * sizeof(T) + ny * sizeof(T) +
+                (size_t)ny * 3 * sizeof(double) + ECAP * sizeof(double) + sizeof(Scalars);
+
+    HostTables<T> t;
+    StepArgs<T> &a = args_of<T>(h);
+    host_setup<T>(p, t, a, ECAP);
+    CK(h, cudaMemcpyAsync(h->twx, t.twx.data(), nx * sizeof(cpx<T>), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->twy, t.twy.data(), ny * sizeof(cpx<T>), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->kxt, t.kx.data(), t.kx.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->kyt, t.ky.data(), t.ky.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    a.u0 = (cpx<T> *)h->u0;
+    a.acc = (cpx<T> *)h->acc;
+    a.fa = (cpx<T> *)h->fa;
+    a.fx = (cpx<T> *)h->fx;
+    a.fy = (cpx<T> *)h->fy;
+    a.P = (cpx<T> *)h->P;
+    a.Q = (cpx<T> *)h->Q;
+    a.twx = (const cpx<T> *)h->twx;
+    a.twy = (const cpx<T> *)h->twy;
+    a.kxt = (const T *)h->kxt;
+    a.kyt = (const T *)h->kyt;
+    a.rowp = h->rowp;
+    a.sc = h->sc;
+    a.energy = h->energy;
+
+    // Opt in to large dynamic shared memory where needed.
+    const KernelTable<T> &K = table<T>();
+    struct {
+        const void *fn;
+        size_t smem;
+    } ks[] = {{(const void *)K.row[h->lognx], K.row_shape[h->lognx].smem},
+              {(const void *)K.col[h->logny], K.col_shape[h->logny].smem},
+              {(const void *)K.rowfwd[h->lognx], K.rowfwd_shape[h->lognx].smem},
+              {(const void *)K.colfwd[h->logny], K.colfwd_shape[h->logny].smem}};
+    for (auto &k : ks) {
+        if (k.smem > 48 * 1024)
+            CK(h, cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem));
+    }
+    return AM_OK;
+}
+
+template <typename T>
+static am_status launch_col(am_handle *h, int mode)
+{
+    const KernelTable<T> &K = table<T>();
+    StepArgs<T> a = args_of<T>(h);
+    a.mode = mode;
+    const LaunchShape &s = K.col_shape[h->logny];
+    int grid = (h->nt + s.per_block - 1) / s.per_block;
+    K.col[h->logny]<<<grid, s.threads, s.smem, h->stream>>>(a);
+    CK(h, cudaGetLastError());
+    return AM_OK;
+}
+
+template <typename T>
+static am_status launch_row(am_handle *h)
+{
+    const KernelTable<T> &K = table<T>();
+    const LaunchShape &s = K.row_shape[h->lognx];
+    int grid = (h->p.ny + s.per_block - 1) / s.per_block;
+    K.row[h->lognx]<<<grid, s.threads, s.smem, h->stream>>>(args_of<T>(h));
+    CK(h, cudaGetLastError());
+    return AM_OK;
+}
+
+template <typename T>
+static am_status enqueue_step(am_handle *h)
+{
+    for (int s = 1; s <= 4; s++) {
+        am_status st = launch_row<T>(h);
+        if (st) return st;
+        st = launch_col<T>(h, s);
+        if (st) return st;
+    }
+    return AM_OK;
+}
+
+template <typename T>
+static am_status build_graph(am_handle *h)
+{
+    if (h->graph) return AM_OK;
+    cudaGraph_t g;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    am_status st = enqueue_step<T>(h);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    return AM_OK;
+}
+
+static am_status reset_scalars(am_handle *h, const double mean[2])
+{
+    Scalars s{};
+    s.m_new[0] = mean ? mean[0] : 0.0;
+    s.m_new[1] = mean ? mean[1] : 0.0;
+    s.m_old[0] = s.m_appr[0] = s.m_new[0];
+    s.m_old[1] = s.m_appr[1] = s.m_new[1];
+    s.step = 0;
+    s.nan_step = -1;
+    CK(h, cudaMemcpyAsync(h->sc, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return AM_OK;
+}
+
+template <typename T>
+static am_status set_state_impl(am_handle *h, const void *w_hat, const double mean[2])
+{
+    const size_t bytes = (size_t)h->p.ny * h->nxh * sizeof(cpx<T>);
+    CK(h, cudaMemcpyAsync(h->stage, w_hat, bytes, cudaMemcpyHostToDevice, h->stream));
+    table<T>().tile<<<1024, 256, 0, h->stream>>>((const cpx<T> *)h->stage, (cpx<T> *)h->u0, h->p.ny, h->nxh,
+                                                 h->nt);
+    CK(h, cudaGetLastError());
+    am_status st = reset_scalars(h, mean);
+    if (st) return st;
+    st = launch_col<T>(h, 0);
+    if (st) return st;
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->state_loaded = true;
+    return AM_OK;
+}
+
+template <typename T>
+static am_status set_state_real_impl(am_handle *h, const void *w_real, const double mean[2], int mask)
+{
+    const KernelTable<T> &K = table<T>();
+    const size_t bytes = (size_t)h->p.ny * h->p.nx * sizeof(T);
+    CK(h, cudaMemcpyAsync(h->stage, w_real, bytes, cudaMemcpyHostToDevice, h->stream));
+    const LaunchShape &rs = K.rowfwd_shape[h->lognx];
+    K.rowfwd[h->lognx]<<<(h->p.ny + rs.per_block - 1) / rs.per_block, rs.threads, rs.smem, h->stream>>>(
+        (const T *)h->stage, (cpx<T> *)h->P, (const cpx<T> *)h->twx, h->p.ny, h->nt);
+    CK(h, cudaGetLastError());
+    const LaunchShape &cs = K.colfwd_shape[h->logny];
+    K.colfwd[h->logny]<<<(h->nt + cs.per_block - 1) / cs.per_block, cs.threads, cs.smem, h->stream>>>(
+        (const cpx<T> *)h->P, (cpx<T> *)h->u0, (const cpx<T> *)h->twy, h->p.nx, h->p.ny, h->nxh, h->nt, mask,
+        h->p.dealias, args_of<T>(h).rsq);
+    CK(h, cudaGetLastError());
+    am_status st = reset_scalars(h, mean);
+    if (st) return st;
+    st = launch_col<T>(h, 0);
+    if (st) return st;
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->state_loaded = true;
+    return AM_OK;
+}
+
+template <typename T>
+static am_status get_state_impl(am_handle *h, void *w_hat, double mean[2])
+{
+    table<T>().untile<<<1024, 256, 0, h->stream>>>((const cpx<T> *)h->u0, (cpx<T> *)h->stage, h->p.ny, h->nxh,
+                                                   h->nt);
+    CK(h, cudaGetLastError());
+    const size_t bytes = (size_t)h->p.ny * h->nxh * sizeof(cpx<T>);
+    if (w_hat) CK(h, cudaMemcpyAsync(w_hat, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream));
+    Scalars s;
+    CK(h, cudaMemcpyAsync(&s, h->sc, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (mean) {
+        mean[0] = s.m_new[0];
+        mean[1] = s.m_new[1];
+    }
+    return AM_OK;
+}
+
+template <typename T>
+static am_status step_impl(am_handle *h, int nsteps, double *energy, int *nan_step, bool wait)
+{
+    if (nan_step) *nan_step = -1;
+    am_status st = build_graph<T>(h);
+    if (st) return st;
+    if (!wait) {
+        for (int i = 0; i < nsteps; i++) CK(h, cudaGraphLaunch(h->graph, h->stream));
+        return AM_OK;
+    }
+    int done = 0;
+    while (done < nsteps) {
+        int k = nsteps - done < ECAP ? nsteps - done : ECAP;
+        CK(h, cudaMemsetAsync(&h->sc->step, 0, sizeof(int), h->stream));
+        for (int i = 0; i < k; i++) CK(h, cudaGraphLaunch(h->graph, h->stream));
+        if (energy)
+            CK(h, cudaMemcpyAsync(energy + done, h->energy, k * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        Scalars s;
+        CK(h, cudaMemcpyAsync(&s, h->sc, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        if (s.nan_step >= 0) {
+            if (nan_step) *nan_step = done + s.nan_step;
+            h->err = "w(0,0) is NaN after step " + std::to_string(done + s.nan_step);
+            return AM_ERR_NAN;
+        }
+        done += k;
+    }
+    return AM_OK;
+}
+
+// ------------------------------------------------------------------- C ABI
+
+extern "C" {
+
+const char *am_status_string(am_status s)
+{
+    switch (s) {
+    case AM_OK: return "ok";
+    case AM_ERR_ARG: return "invalid argument";
+    case AM_ERR_CUDA: return "CUDA error";
+    case AM_ERR_NAN: return "array contains nan values";
+    case AM_ERR_IO: return "I/O error";
+    case AM_ERR_SPEC: return "specification error";
+    case AM_ERR_OOM: return "out of device memory";
+    case AM_ERR_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown status";
+}
+
+const char *am_last_error(const am_handle *h) { return h ? h->err.c_str() : ""; }
+
+int am_mask_value(int nx, int ny, int dealias, int ix, int iy)
+{
+    return mask_at(dealias, reference_rsq(nx, ny), nx, ny, ix, iy);
+}
+
+am_status am_create(const am_params *p, am_handle **out)
+{
+    if (!p || !out) return AM_ERR_ARG;
+    *out = nullptr;
+    if (!is_pow2(p->nx) || !is_pow2(p->ny) || p->nx < (1 << LOG_MIN) || p->ny < (1 << LOG_MIN) ||
+        p->nx > (1 << LOG_MAX) || p->ny > (1 << LOG_MAX))
+        return AM_ERR_UNSUPPORTED;
+    if (p->precision != AM_FP32 && p->precision != AM_FP64) return AM_ERR_ARG;
+    if (p->dealias < 0 || p->dealias > 2 || (p->form != AM_FORM_REFERENCE && p->form != AM_FORM_GENERAL))
+        return AM_ERR_ARG;
+    if (!(p->lx > 0) || !(p->ly > 0) || !std::isfinite(p->dt)) return AM_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return AM_ERR_CUDA;
+    am_handle *h = new (std::nothrow) am_handle();
+    if (!h) return AM_ERR_OOM;
+    h->p = *p;
+    h->fp64 = p->precision == AM_FP64;
+    h->lognx = ilog2(p->nx);
+    h->logny = ilog2(p->ny);
+    cudaGetDevice(&h->device);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return AM_ERR_CUDA;
+    }
+    h->own_stream = true;
+    am_status st = h->fp64 ? alloc_and_tables<double>(h) : alloc_and_tables<float>(h);
+    if (st) {
+        am_destroy(h);
+        return st;
+    }
+    *out = h;
+    return AM_OK;
+}
+
+am_status am_destroy(am_handle *h)
+{
+    if (!h) return AM_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    void *ptrs[] = {h->u0, h->acc, h->fa, h->fx, h->fy, h->P, h->Q, h->stage, h->twx, h->twy,
+                    h->kxt, h->kyt, h->rowp, h->energy, h->sc};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return AM_OK;
+}
+
+am_status am_set_stream(am_handle *h, void *stream)
+{
+    if (!h) return AM_ERR_ARG;
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    if (stream) {
+        if (h->own_stream) cudaStreamDestroy(h->stream);
+        h->own_stream = false;
+        h->stream = (cudaStream_t)stream;
+    } else if (!h->own_stream) {
+        CK(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        h->own_stream = true;
+    }
+    return AM_OK;
+}
+
+am_status am_set_state(am_handle *h, const void *w_hat, const double mean[2])
+{
+    if (!h || !w_hat) return AM_ERR_ARG;
+    return h->fp64 ? set_state_impl<double>(h, w_hat, mean) : set_state_impl<float>(h, w_hat, mean);
+}
+
+am_status am_set_state_real(am_handle *h, const void *w_real, const double mean[2], int mask_and_zero_mean)
+{
+    if (!h || !w_real) return AM_ERR_ARG;
+    return h->fp64 ? set_state_real_impl<double>(h, w_real, mean, mask_and_zero_mean)
+                   : set_state_real_impl<float>(h, w_real, mean, mask_and_zero_mean);
+}
+
+am_status am_get_state(am_handle *h, void *w_hat, double mean[2])
+{
+    if (!h) return AM_ERR_ARG;
+    if (!h->state_loaded) {
+        h->err = "no state loaded";
+        return AM_ERR_ARG;
+    }
+    return h->fp64 ? get_state_impl<double>(h, w_hat, mean) : get_state_impl<float>(h, w_hat, mean);
+}
+
+am_status am_step(am_handle *h, int nsteps, double *energy, int *nan_step)
+{
+    if (!h || nsteps < 0) return AM_ERR_ARG;
+    if (!h->state_loaded) {
+        h->err = "no state loaded";
+        return AM_ERR_ARG;
+    }
+    return h->fp64 ? step_impl<double>(h, nsteps, energy, nan_step, true)
+                   : step_impl<float>(h, nsteps, energy, nan_step, true);
+}
+
+am_status am_step_async(am_handle *h, int nsteps)
+{
+    if (!h || nsteps < 0) return AM_ERR_ARG;
+    if (!h->state_loaded) return AM_ERR_ARG;
+    return h->fp64 ? step_impl<double>(h, nsteps, nullptr, nullptr, false)
+                   : step_impl<float>(h, nsteps, nullptr, nullptr, false);
+}
+
+am_status am_sync(am_handle *h)
+{
+    if (!h) return AM_ERR_ARG;
+    Scalars s;
+    CK(h, cudaMemcpyAsync(&s, h->sc, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (s.nan_step >= 0) return AM_ERR_NAN;
+    return AM_OK;
+}
+
+am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double col_ms[4])
+{
+    if (!h || nsteps < 0 || !row_ms || !col_ms) return AM_ERR_ARG;
+    if (!h->state_loaded) return AM_ERR_ARG;
+    cudaEvent_t ev[9];
+    for (auto &e : ev) CK(h, cudaEventCreate(&e));
+    am_status st = AM_OK;
+    for (int m = 0; m < nsteps && !st; m++) {
+        CK(h, cudaEventRecord(ev[0], h->stream));
+        for (int s = 1; s <= 4 && !st; s++) {
+            st = h->fp64 ? launch_row<double>(h) : launch_row<float>(h);
+            if (!st) CK(h, cudaEventRecord(ev[2 * s - 1], h->stream));
+            if (!st) st = h->fp64 ? launch_col<double>(h, s) : launch_col<float>(h, s);
+            if (!st) CK(h, cudaEventRecord(ev[2 * s], h->stream));
+        }
+        if (st) break;
+        CK(h, cudaEventSynchronize(ev[8]));
+        for (int s = 1; s <= 4; s++) {
+            float a = 0, b = 0;
+            CK(h, cudaEventElapsedTime(&a, ev[2 * s - 2], ev[2 * s - 1]));
+            CK(h, cudaEventElapsedTime(&b, ev[2 * s - 1], ev[2 * s]));
+            row_ms[s - 1] += a;
+            col_ms[s - 1] += b;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return st;
+}
+
+int am_launches_per_step(const am_handle *h) { return h ? 8 : 0; }
+
+long long am_device_bytes(const am_handle *h) { return h ? h->bytes : 0; }
+
+am_status am_ic_bandlimited(int nx, int ny, unsigned long long seed, double kmin, double kmax, double rms,
+                            double *w_hat)
+{
+    if (!w_hat || nx < 4 || ny < 4 || kmax < 0 || 2 * kmax >= nx || 2 * kmax >= ny) return AM_ERR_ARG;
+    const int nxh = nx / 2 + 1;
+    std::memset(w_hat, 0, sizeof(double) * 2 * (size_t)ny * nxh);
+    std::mt19937_64 gen(seed);
+    auto unit = [&gen]() { return (double)(gen() >> 11) * (1.0 / 9007199254740992.0); };
+    const int km = (int)std::floor(kmax);
+    const double kmin2 = kmin * kmin, kmax2 = kmax * kmax;
+    for (int iy = -km; iy <= km; iy++) {
+        for (int ix = 0; ix <= km; ix++) {
+            if (ix == 0 && iy <= 0) continue;
+            double r2 = (double)(ix * ix + iy * iy);
+            if (r2 < kmin2 || r2 > kmax2) continue;
+            double u1 = unit(), u2 = unit(), u3 = unit();
+            double amp = std::sqrt(-2.0 * std::log(1.0 - u1)) * std::cos(2.0 * M_PI * u2);
+            double ph = 2.0 * M_PI * u3;
+            double re = amp * std::cos(ph), im = amp * std::sin(ph);
+            size_t k = ((size_t)((iy % ny + ny) % ny) * nxh + ix) * 2;
+            w_hat[k] = re;
+            w_hat[k + 1] = im;
+            if (ix == 0) {
+                size_t kc = ((size_t)((-iy % ny + ny) % ny) * nxh) * 2;
+                w_hat[kc] = re;
+                w_hat[kc + 1] = -im;
+            }
+        }
+    }
+    // Scale to the requested real-space rms (Parseval on the full plane).
+    double full = 0;
+    for (int iy = 0; iy < ny; iy++)
+        for (int ix = 0; ix < nxh; ix++) {
+            size_t k = ((size_t)iy * nxh + ix) * 2;
+            double a2 = w_hat[k] * w_hat[k] + w_hat[k + 1] * w_hat[k + 1];
+            full += (ix == 0 ? 1.0 : 2.0) * a2;
+        }
+    double cur = std::sqrt(full) / ((double)nx * ny);
+    if (cur > 0) {
+        double f = rms / cur;
+        for (size_t k = 0; k < (size_t)2 * ny * nxh; k++) w_hat[k] *= f;
+    }
+    return AM_OK;
+}
+
+}  // extern "C"

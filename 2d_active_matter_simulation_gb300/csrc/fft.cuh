@@ -1,0 +1,248 @@
+// Shared-memory Stockham FFT building blocks for the actflow step kernels.
+//
+// The same source compiles as CUDA device code (nvcc, sm_103a) and as plain C++
+// (g++), so the test suite can execute the kernels' per-thread logic on the CPU
+// with real threads and barriers.  Only the qualifier macros differ.
+//
+// Conventions
+//  * cpx<T>: complex number {x = real, y = imaginary}, T = float or double.
+//  * A length-L transform is computed by TPC = L/R threads; thread j holds the
+//    elements j + r*TPC (r = 0..R-1) in registers on entry and on exit
+//    ("cyclic distribution").  The first pass may use a smaller radix R1 (each
+//    thread then runs R/R1 butterflies); every later pass has radix R.
+//  * Pass with sub-transform size Ns (Stockham autosort, decimation in time,
+//    as in Govindaraju et al., "High performance discrete Fourier transforms on
+//    graphics processors", SC 2008): thread j reads x[j + r*TPC], multiplies by
+//    W_{Ns R}^{r (j mod Ns)}, runs an R-point DFT and writes y[(j/Ns) Ns R +
+//    (j mod Ns) + r Ns].  The last pass keeps its outputs in registers, which
+//    for Ns = L/R are exactly y[j + r*TPC].
+//  * Transforms are unnormalised; SIGN = -1 forward, +1 inverse.
+#pragma once
+
+#ifdef __CUDACC__
+#define AF_HD __host__ __device__ __forceinline__
+#define AF_HDC __host__ __device__
+#define AF_DEV __device__ __forceinline__
+#else
+#include <math.h>
+
+#include <cmath>
+#define AF_HD inline
+#define AF_HDC
+#define AF_DEV inline
+#endif
+
+namespace af {
+
+template <typename T>
+struct alignas(2 * sizeof(T)) cpx {
+    T x, y;
+};
+
+template <typename T>
+AF_HD cpx<T> mk(T a, T b)
+{
+    cpx<T> r;
+    r.x = a;
+    r.y = b;
+    return r;
+}
+template <typename T>
+AF_HD cpx<T> operator+(cpx<T> a, cpx<T> b) { return mk(a.x + b.x, a.y + b.y); }
+template <typename T>
+AF_HD cpx<T> operator-(cpx<T> a, cpx<T> b) { return mk(a.x - b.x, a.y - b.y); }
+template <typename T>
+AF_HD cpx<T> cmul(cpx<T> a, cpx<T> b) { return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+// a * conj(b)
+template <typename T>
+AF_HD cpx<T> cmulc(cpx<T> a, cpx<T> b) { return mk(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
+template <typename T>
+AF_HD cpx<T> conj(cpx<T> a) { return mk(a.x, -a.y); }
+template <typename T>
+AF_HD cpx<T> scale(cpx<T> a, T s) { return mk(a.x * s, a.y * s); }
+
+// Multiply by exp(SIGN * 2 pi i Q / R) for compile-time Q, R (R <= 16).
+// Multiples of pi/2 are exact sign swaps; the remaining angles are multiples
+// of pi/8, whose cosines and sines are the constants below.
+template <int Q, int R, int SIGN, typename T>
+AF_HD cpx<T> rot(cpx<T> a)
+{
+    constexpr int N16 = (16 / R) * Q;          // angle in units of 2 pi / 16
+    constexpr int q = ((N16 % 16) + 16) % 16;
+    if constexpr (q == 0) {
+        return a;
+    } else if constexpr (q == 4) {             // pi/2: multiply by SIGN * i
+        return SIGN > 0 ? mk(-a.y, a.x) : mk(a.y, -a.x);
+    } else if constexpr (q == 8) {
+        return mk(-a.x, -a.y);
+    } else if constexpr (q == 12) {
+        return SIGN > 0 ? mk(a.y, -a.x) : mk(-a.y, a.x);
+    } else {
+        // cos and sin of 2 pi k / 16 for k = 0..3 (first quadrant)
+        constexpr double C[4] = {1.0, 0.92387953251128675613, 0.70710678118654752440, 0.38268343236508977173};
+        constexpr int qq = q % 4;               // offset inside the quadrant
+        constexpr int quad = q / 4;
+        // cos(q*2pi/16), sin(q*2pi/16) from quadrant symmetry
+        constexpr double c0 = C[qq], s0 = C[4 - qq == 4 ? 0 : 4 - qq];
+        constexpr double cs = quad == 0 ? c0 : quad == 1 ? -s0 : quad == 2 ? -c0 : s0;
+        constexpr double sn = quad == 0 ? s0 : quad == 1 ? c0 : quad == 2 ? -s0 : -c0;
+        const T c = (T)cs, s = (T)(SIGN * sn);
+        return mk(a.x * c - a.y * s, a.x * s + a.y * c);
+    }
+}
+
+// In-register R-point DFT, natural order in and out (radix-2 decimation in
+// time, fully unrolled at compile time).
+template <int R, int SIGN, typename T>
+struct DFT {
+    static AF_HD void run(cpx<T> *v)
+    {
+        if constexpr (R == 1) {
+            return;
+        } else if constexpr (R == 2) {
+            cpx<T> a = v[0], b = v[1];
+            v[0] = a + b;
+            v[1] = a - b;
+        } else {
+            cpx<T> e[R / 2], o[R / 2];
+#pragma unroll
+            for (int i = 0; i < R / 2; i++) {
+                e[i] = v[2 * i];
+                o[i] = v[2 * i + 1];
+            }
+            DFT<R / 2, SIGN, T>::run(e);
+            DFT<R / 2, SIGN, T>::run(o);
+            combine<0>(v, e, o);
+        }
+    }
+    template <int Q>
+    static AF_HD void combine(cpx<T> *v, const cpx<T> *e, const cpx<T> *o)
+    {
+        if constexpr (Q < R / 2) {
+            cpx<T> t = rot<Q, R, SIGN, T>(o[Q]);
+            v[Q] = e[Q] + t;
+            v[Q + R / 2] = e[Q] - t;
+            combine<Q + 1>(v, e, o);
+        }
+    }
+};
+
+// Shared-memory exchange buffer for W interleaved transforms (W columns of a
+// tile, or W = 1 for a single row).  Real and imaginary parts live in separate
+// arrays; element idx of transform c sits at word PAD(idx) * W + c.  The padding
+// functions were chosen by simulating the bank pattern of every pass.
+template <typename T, int W, int PADK>
+struct XBuf {
+    T *re, *im;
+    AF_HDC static constexpr int pad(int i)
+    {
+        if constexpr (PADK == 36) return i + (i >> 3) + (i >> 6);
+        else return i + (i >> PADK);
+    }
+    AF_HDC static constexpr int words(int L) { return pad(L - 1) * W + W; }
+    AF_HD int w(int idx, int c) const { return pad(idx) * W + c; }
+    AF_HD void put(int idx, int c, cpx<T> v) const
+    {
+        int k = w(idx, c);
+        re[k] = v.x;
+        im[k] = v.y;
+    }
+    AF_HD cpx<T> get(int idx, int c) const
+    {
+        int k = w(idx, c);
+        return mk(re[k], im[k]);
+    }
+};
+
+// Twiddle source: tw[m * STRIDE] = exp(-2 pi i m / L) for m < L.
+AF_HD cpx<float> ldtw(const cpx<float> *tw, int idx)
+{
+#ifdef __CUDA_ARCH__
+    float2 v = __ldg(reinterpret_cast<const float2 *>(tw) + idx);
+    return mk(v.x, v.y);
+#else
+    return tw[idx];
+#endif
+}
+AF_HD cpx<double> ldtw(const cpx<double> *tw, int idx)
+{
+#ifdef __CUDA_ARCH__
+    double2 v = __ldg(reinterpret_cast<const double2 *>(tw) + idx);
+    return mk(v.x, v.y);
+#else
+    return tw[idx];
+#endif
+}
+
+// Length-L (L = 2^LOGL) block FFT on data distributed cyclically over TPC =
+// L/R threads.  `sync` is the block barrier (called identically by every
+// thread of the block).  tw must hold exp(-2 pi i m / (L * TWS)) at index m for
+// m < L * TWS; the transform uses every TWS-th entry.
+template <typename T, int LOGL, int LOGR_MAX, int SIGN>
+struct BlockFFT {
+    static constexpr int LOGR = LOGR_MAX < LOGL ? LOGR_MAX : LOGL;
+    static constexpr int R = 1 << LOGR;
+    static constexpr int L = 1 << LOGL;
+    static constexpr int TPC = L / R;
+    static constexpr int LOGR1 = LOGL % LOGR;
+    static constexpr int R1 = 1 << LOGR1;          // first-pass radix (1: none)
+    static constexpr int NPASS = (LOGL - LOGR1) / LOGR;
+
+    template <class Buf, class Sync>
+    static AF_HD void run(cpx<T> (&v)[R], int j, int c, const Buf &buf, const cpx<T> *tw, int TWS, Sync &&sync)
+    {
+        int Ns = 1;
+        bool in_regs = true;
+        if constexpr (LOGR1 > 0) {
+            constexpr int G = R / R1;
+#pragma unroll
+            for (int q = 0; q < G; q++) {
+                cpx<T> u[R1];
+#pragma unroll
+                for (int r1 = 0; r1 < R1; r1++) u[r1] = v[q + G * r1];
+                DFT<R1, SIGN, T>::run(u);
+#pragma unroll
+                for (int r1 = 0; r1 < R1; r1++) v[q + G * r1] = u[r1];
+            }
+            sync();
+#pragma unroll
+            for (int q = 0; q < G; q++) {
+                int b = j + q * TPC;
+#pragma unroll
+                for (int r1 = 0; r1 < R1; r1++) buf.put(b * R1 + r1, c, v[q + G * r1]);
+            }
+            sync();
+            Ns = R1;
+            in_regs = false;
+        }
+#pragma unroll
+        for (int p = 0; p < NPASS; p++) {
+            if (!in_regs) {
+#pragma unroll
+                for (int r = 0; r < R; r++) v[r] = buf.get(j + r * TPC, c);
+            }
+            in_regs = false;
+            if (Ns > 1) {
+                int k = j & (Ns - 1);
+                int step = (L / (Ns * R)) * k * TWS;   // twiddle index of W^{k}
+#pragma unroll
+                for (int r = 1; r < R; r++) {
+                    cpx<T> w = ldtw(tw, r * step);
+                    v[r] = SIGN < 0 ? cmul(v[r], w) : cmulc(v[r], w);
+                }
+            }
+            DFT<R, SIGN, T>::run(v);
+            if (p < NPASS - 1) {
+                int k = j & (Ns - 1);
+                int base = (j - k) * R + k;
+                sync();
+#pragma unroll
+                for (int r = 0; r < R; r++) buf.put(base + r * Ns, c, v[r]);
+                sync();
+                Ns *= R;
+            }
+        }
+    }
+};
+
+}  // namespace af

@@ -1,0 +1,88 @@
+// Host-side set-up of one simulation: twiddle and wavenumber tables and the
+// scalar kernel arguments.  Shared by the C ABI (actflow_api.cu) and the test
+// suite's CPU execution of the kernel bodies, so both run identical set-up.
+#pragma once
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "actflow.h"
+#include "step_kernels.cuh"
+
+namespace af {
+
+// Reference dealias radius: (Nxh-1)*(Nxh-1)*Ny*Ny/4 in 32-bit int arithmetic
+// (ActFlow_V3-2.cu:911); the products wrap modulo 2^32 on the GPU.
+inline int reference_rsq(int nx, int ny)
+{
+    int nxh = nx / 2 + 1;
+    uint32_t r = (uint32_t)(nxh - 1) * (uint32_t)(nxh - 1);
+    r *= (uint32_t)ny;
+    r *= (uint32_t)ny;
+    return (int32_t)r / 4;
+}
+
+template <typename T>
+struct HostTables {
+    int nxh = 0, nt = 0;
+    std::vector<cpx<T>> twx, twy;   // exp(-2 pi i m / N)
+    std::vector<T> kx, ky;          // kx padded to nt * W entries
+};
+
+// Fill the tables and every scalar field of `a` (pointers are left alone).
+template <typename T>
+void host_setup(const am_params &p, HostTables<T> &t, StepArgs<T> &a, int ecap)
+{
+    const int nx = p.nx, ny = p.ny;
+    const int W = Tile<T>::W;
+    t.nxh = nx / 2 + 1;
+    t.nt = (t.nxh + W - 1) / W;
+    // Twiddles, computed in double and rounded to T.
+    t.twx.resize(nx);
+    t.twy.resize(ny);
+    for (int m = 0; m < nx; m++) {
+        double ang = -2.0 * M_PI * (double)m / nx;
+        t.twx[m] = mk((T)std::cos(ang), (T)std::sin(ang));
+    }
+    for (int m = 0; m < ny; m++) {
+        double ang = -2.0 * M_PI * (double)m / ny;
+        t.twy[m] = mk((T)std::cos(ang), (T)std::sin(ang));
+    }
+    // Wavenumbers 2 pi / L * n (wavenumber_func, ActFlow_V3-2.cu:1329-1349):
+    // the box length is held in T (the reference parses it into a float), the
+    // product is formed in double and rounded to T.  Rows are in FFT order.
+    t.kx.assign((size_t)t.nt * W, (T)0);
+    t.ky.resize(ny);
+    const double lx = (double)(T)p.lx, ly = (double)(T)p.ly;
+    for (int i = 0; i < t.nxh; i++) t.kx[i] = (T)(2.0 * M_PI / lx * i);
+    for (int i = 0; i < ny; i++) t.ky[i] = (T)(2.0 * M_PI / ly * (i < ny / 2 + 1 ? i : i - ny));
+
+    a.nx = nx;
+    a.ny = ny;
+    a.nxh = t.nxh;
+    a.nt = t.nt;
+    a.ecap = ecap;
+    // FFT normalisation folded into lambda and beta in T, as the reference does
+    // (ActFlow_V3-2.cu:434-436): lambda / N^2, beta / N^3.
+    const T fnorm = (T)(nx * ny);
+    a.lam_s = (T)p.lambda / (fnorm * fnorm);
+    a.beta_s = (T)p.beta / (fnorm * fnorm * fnorm);
+    const double nd = (double)nx * (double)ny;
+    a.beta_sd = p.beta / (nd * nd * nd);
+    a.dt = (T)p.dt;
+    a.alpha = (T)p.alpha;
+    a.g0 = (T)p.gamma0;
+    a.g2 = (T)p.gamma2;
+    a.form = p.form;
+    a.dealias = p.dealias;
+    a.rsq = reference_rsq(nx, ny);
+    // Mean-flow integrating factors exp(L(0) dt), exp(L(0) dt / 2), in double
+    // (the reference evaluates them in float, ActFlow_V3-2.cu:704-705).
+    const double L0 = p.form == AM_FORM_REFERENCE ? -(1.0 + p.alpha) : -p.alpha;
+    a.lin_v = std::exp(L0 * p.dt);
+    a.lin2_v = std::exp(L0 * p.dt / 2);
+    a.inv_2n3 = 1.0 / (2.0 * nd * nd * nd);
+    a.mode = 0;
+}
+
+}  // namespace af

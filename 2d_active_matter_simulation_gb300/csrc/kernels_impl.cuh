@@ -1,0 +1,93 @@
+// Kernel entry points and dispatch-table construction, included once per
+// precision by kernels_f32.cu and kernels_f64.cu.
+#pragma once
+#include "kernels.h"
+#include "setup_kernels.cuh"
+
+namespace af {
+
+template <typename T, int LOG>
+__global__ void __launch_bounds__(RowPass<T, LOG>::THREADS) k_row(StepArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    RowPass<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+}
+
+template <typename T, int LOG>
+__global__ void __launch_bounds__(ColPass<T, LOG>::THREADS) k_col(StepArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    ColPass<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+}
+
+template <typename T, int LOG>
+__global__ void __launch_bounds__(RowFwd<T, LOG>::THREADS)
+    k_rowfwd(const T *src, cpx<T> *dst, const cpx<T> *twx, int ny, int nt)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    RowFwd<T, LOG>::body(src, dst, twx, ny, nt, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+}
+
+template <typename T, int LOG>
+__global__ void __launch_bounds__(ColFwd<T, LOG>::THREADS)
+    k_colfwd(const cpx<T> *src, cpx<T> *dst, const cpx<T> *twy, int nx, int ny, int nxh, int nt, int apply_mask,
+             int dealias, int rsq)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    ColFwd<T, LOG>::body(src, dst, twy, nx, ny, nxh, nt, apply_mask, dealias, rsq, threadIdx.x, blockIdx.x, smem,
+                         []() { __syncthreads(); });
+}
+
+// Reference half-plane layout [ny][nxh] <-> tiled layout; padding columns zero.
+template <typename T>
+__global__ void k_tile(const cpx<T> *src, cpx<T> *dst, int ny, int nxh, int nt)
+{
+    constexpr int W = Tile<T>::W;
+    size_t total = (size_t)nt * W * ny;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        int c = (int)(i % W);
+        size_t rest = i / W;
+        int y = (int)(rest % ny);
+        int t = (int)(rest / ny);
+        int kx = t * W + c;
+        dst[i] = kx < nxh ? src[(size_t)y * nxh + kx] : mk<T>(0, 0);
+    }
+}
+
+template <typename T>
+__global__ void k_untile(const cpx<T> *src, cpx<T> *dst, int ny, int nxh, int nt)
+{
+    size_t total = (size_t)ny * nxh;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        int y = (int)(i / nxh), kx = (int)(i % nxh);
+        dst[i] = src[tidx<T>(kx, y, ny)];
+    }
+}
+
+template <typename T, int LOG>
+struct Fill {
+    static void run(KernelTable<T> &t)
+    {
+        t.row[LOG] = k_row<T, LOG>;
+        t.row_shape[LOG] = {RowPass<T, LOG>::THREADS, RowPass<T, LOG>::smem_bytes(), RowPass<T, LOG>::ROWS};
+        t.col[LOG] = k_col<T, LOG>;
+        t.col_shape[LOG] = {ColPass<T, LOG>::THREADS, ColPass<T, LOG>::smem_bytes(), ColPass<T, LOG>::TILES};
+        t.rowfwd[LOG] = k_rowfwd<T, LOG>;
+        t.rowfwd_shape[LOG] = {RowFwd<T, LOG>::THREADS, RowFwd<T, LOG>::smem_bytes(), RowFwd<T, LOG>::ROWS};
+        t.colfwd[LOG] = k_colfwd<T, LOG>;
+        t.colfwd_shape[LOG] = {ColFwd<T, LOG>::THREADS, ColFwd<T, LOG>::smem_bytes(), ColFwd<T, LOG>::TILES};
+        if constexpr (LOG < LOG_MAX) Fill<T, LOG + 1>::run(t);
+    }
+};
+
+template <typename T>
+KernelTable<T> make_table()
+{
+    KernelTable<T> t{};
+    Fill<T, LOG_MIN>::run(t);
+    t.tile = k_tile<T>;
+    t.untile = k_untile<T>;
+    return t;
+}
+
+}  // namespace af

@@ -1,0 +1,290 @@
+"""Benchmark: grid-point-steps/s of the IF-RK4 vorticity step on one GB300.
+
+Workload (the configuration the headline metric is quoted on): one 2048^2
+simulation, FP32, dt = 1e-4 on the [0, 2 pi)^2 box, lambda = 3.5, alpha = -0.8,
+beta = 0.01, Gamma0 = -0.045, Gamma2 = 2.5e-5, isotropic 1/2-rule dealiasing,
+seeded band-limited initial field (modes 1 <= |k| <= 8, rms 0.01, seed 7).
+A bench "step" is one full RK4 step (8 kernels: row pass + column pass per
+stage).
+
+    python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm times K steps with CUDA events on the solver's stream (state resident
+in HBM, L2 flushed by a 256 MB write before every step), then the same metric
+end to end through the C ABI with host buffers (set_state from pinned memory,
+K steps with the per-step energy read back, get_state), per-kernel CUDA-event
+times for the roofline, and the oracle's CPU step as the reported CPU baseline.
+The reference arm times the CPU implementation of the step (the oracle, a C
+restatement of the reference program's step; the reference itself has no CPU
+path) on all host cores, one full 2048^2 step per bench step.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX = NY = 2048
+PARAMS = dict(lx=2 * math.pi, ly=2 * math.pi, dt=1e-4, lam=3.5, alpha=-0.8, beta=0.01,
+              gamma0=-0.045, gamma2=2.5e-5, dealias="half")
+SEED = 7
+WORKLOAD = "IF-RK4 vorticity step, 2048^2, FP32, dt=1e-4, 1/2-rule dealiasing, band-limited seed 7"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                       "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.p is None:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def oracle_steps(nsteps, threads=0):
+    """Time `nsteps` full oracle steps of the workload on host cores."""
+    import numpy as np
+    import oracle
+    import importlib
+    am = importlib.import_module("2d_active_matter_simulation_gb300")
+    w0 = am.ic_bandlimited(NX, NY, SEED).astype(np.complex64)
+    p = oracle.make_params(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"],
+                           PARAMS["beta"], PARAMS["gamma0"], PARAMS["gamma2"], dealias=PARAMS["dealias"])
+    t = time.perf_counter()
+    oracle.run(p, w0, (0.0, 0.0), nsteps, "f32", nthreads=threads)
+    return time.perf_counter() - t, oracle.num_threads() if threads == 0 else threads
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    oracle.lib()
+    for _ in range(args.warmup):
+        oracle_steps(1)
+    times = []
+    cores = 1
+    for _ in range(args.steps):
+        dt, cores = oracle_steps(1)
+        times.append(dt)
+    total = sum(times)
+    value = NX * NY * args.steps / total
+    out = {
+        "impl": "reference", "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY},
+        "cpu_baseline": {"value": value, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full 2048^2 steps of the oracle (C restatement of "
+                                   "ActFlow_V3-2.cu's step, OpenMP), FP32"},
+        "e2e": {"value": value, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import importlib
+
+    import numpy as np
+    import torch
+
+    am = importlib.import_module("2d_active_matter_simulation_gb300")
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    sim = am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"], PARAMS["beta"],
+                    gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"], precision="fp32")
+    sim.set_stream(stream.cuda_stream)
+    w0 = am.ic_bandlimited(NX, NY, SEED).astype(np.complex64)
+    sim.set_state(w0, (0.0, 0.0))
+
+    # warm-up
+    sim.step_async(max(args.warmup, 0))
+    sim.sync()
+
+    # ---- value: device-resident, CUDA events on the solver's stream
+    clocks = ClockSampler()
+    clocks.start()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            sim.step_async(1)
+            ev[i][1].record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    clk = clocks.stop()
+    sim.sync()
+    total_ms = sum(ms)
+    value = NX * NY * args.steps / (total_ms / 1e3)
+
+    # ---- per-kernel times for the roofline (same stream, L2 flushed per step)
+    row = np.zeros(4)
+    col = np.zeros(4)
+    nprof = max(args.steps, 3)
+    for _ in range(nprof):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        r, c = sim.step_profiled(1)
+        row += r
+        col += c
+    H = NY * (NX // 2 + 1)
+    s = 8
+    row_avg = row.sum() / (4 * nprof)
+    col_avg = col.sum() / (4 * nprof)
+    # algorithmic bytes per launch: row pass 5 fields (3 in, 2 out); column
+    # pass 7, 8, 8, 7 fields in stages 1..4 (mean 7.5)
+    row_bytes = 5 * s * H
+    col_bytes = 7.5 * s * H
+    peak, peak_kind = peaks()
+    if col.sum() >= row.sum():
+        dom, dom_bytes, dom_ms = "column pass (FFT_y, stage update, Biot-Savart, IFFT_y)", col_bytes, col_avg
+    else:
+        dom, dom_bytes, dom_ms = "row pass (C2R_x, products, R2C_x)", row_bytes, row_avg
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    step_bytes = 50 * s * H
+    step_achieved = step_bytes / (total_ms / args.steps / 1e3) / 1e9
+
+    # ---- e2e through the C ABI with host buffers (pinned)
+    w_host = torch.empty((NY, NX // 2 + 1), dtype=torch.complex64, pin_memory=True)
+    w_host.numpy()[:] = w0
+    w_out = torch.empty((NY, NX // 2 + 1), dtype=torch.complex64, pin_memory=True)
+    e_out = torch.empty(args.steps, dtype=torch.float64, pin_memory=True)
+    wh, wo, eo = w_host.numpy(), w_out.numpy(), e_out.numpy()
+    import ctypes
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m = np.zeros(2)
+    am._check(am.lib.am_set_state(sim.h, wh.ctypes.data, am._dptr(np.zeros(2))), sim.h, "set_state")
+    nan_at = ctypes.c_int(-1)
+    am._check(am.lib.am_step(sim.h, args.steps, eo.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                             ctypes.byref(nan_at)), sim.h, "step")
+    am._check(am.lib.am_get_state(sim.h, wo.ctypes.data, am._dptr(m)), sim.h, "get_state")
+    e2e_s = time.perf_counter() - t0
+    e2e_value = NX * NY * args.steps / e2e_s
+    state_bytes = H * s
+    launches = sim.launches_per_step * args.steps
+    sim.close()
+
+    # ---- CPU baseline: the oracle on the host cores, bounded sample
+    cpu = None
+    if not args.no_cpu:
+        n_cpu = 0
+        t_cpu = 0.0
+        cores = 1
+        while t_cpu < 10.0 and n_cpu < 30:
+            dt, cores = oracle_steps(1)
+            t_cpu += dt
+            n_cpu += 1
+        cpu = {"value": NX * NY * n_cpu / t_cpu, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
+               "sample": f"{n_cpu} full 2048^2 steps of the oracle (C restatement of the reference step, "
+                         f"OpenMP, FP32), {t_cpu:.1f} s"}
+
+    out = {
+        "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "dt": PARAMS["dt"], "dealias": "half",
+                   "parallelism": "single GPU", "l2": "flushed before every timed step (256 MB write)",
+                   "timing": "CUDA events on the solver stream, one CUDA graph (8 kernels) per step"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": dom, "algorithmic_bytes_per_launch": dom_bytes,
+                     "avg_launch_ms": dom_ms, "peak_source": peak_kind,
+                     "row_pass_ms": row_avg, "column_pass_ms": col_avg,
+                     "step_achieved_gbs": step_achieved, "step_frac": step_achieved / peak},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "grid-point-steps/s", "h2d_bytes_per_step": state_bytes / args.steps,
+                "d2h_bytes_per_step": (state_bytes + 8 * args.steps) / args.steps,
+                "path": "am_set_state (pinned host) + am_step(K, energy to host) + am_get_state (pinned host)"},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    if args.gpus != 1:
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps({"error": "this solver runs one simulation per GPU; replicas are independent, "
+                                       "run with --gpus 1"}))
+        return
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,185 @@
+/*
+ * actflow -- GB300-native (sm_103a) integrating-factor RK4 step of the 2-D
+ * active-turbulence vorticity equation, behind a plain C ABI.
+ *
+ * Drop-in boundary.  The reference (DominikSuchla/2D_active_matter_simulation,
+ * ActFlow_V3-2.cu) has no library API: its boundary is a process that reads
+ * <dir>/specifications.txt and writes ActTurb_snap{i}.bin and energy.txt.  The
+ * C++ front end `actflow` (csrc/host/cli.cpp) reproduces that process contract;
+ * it, the tests and bench.py drive the solver through the entry points below.
+ * Each entry point names the reference code it replaces.
+ *
+ * Data conventions (identical to the reference's state and snapshot files):
+ *  - w_hat: the vorticity as unnormalised DFT coefficients on the Hermitian half
+ *    plane, row-major [Ny][Nx/2+1] complex (re, im interleaved), rows in FFT
+ *    order ky = 0, 1, ..., Ny/2, -Ny/2+1, ..., -1 (cuFFT R2C output layout,
+ *    ActFlow_V3-2.cu:507, 665; snapshot layout ActFlow_V3-2.cu:1261-1262).
+ *    Element type: float for AM_FP32 handles, double for AM_FP64 handles.
+ *  - mean[2]: the mean velocity scaled by Nx*Ny, i.e. the k = 0 entries of the
+ *    unnormalised velocity spectra (ActFlow_V3-2.cu:1053-1054, 1263).
+ *  - energy: E = sum(ux^2 + uy^2) / (2 (Nx Ny)^3) of the state at the start of
+ *    each step (ActFlow_V3-2.cu:1118-1127), accumulated in double.
+ *
+ * Threading: a handle is not thread-safe; distinct handles are independent.
+ * Every call returns a status and never aborts the process.
+ */
+#ifndef ACTFLOW_H
+#define ACTFLOW_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    AM_OK = 0,
+    AM_ERR_ARG = 1,          /* invalid argument / unsupported size */
+    AM_ERR_CUDA = 2,         /* CUDA runtime error (no device, launch failure) */
+    AM_ERR_NAN = 3,          /* Re w(0,0) became NaN (ActFlow_V3-2.cu:850-861) */
+    AM_ERR_IO = 4,           /* file could not be read or written */
+    AM_ERR_SPEC = 5,         /* malformed specifications.txt / unknown key */
+    AM_ERR_OOM = 6,          /* device allocation failed */
+    AM_ERR_UNSUPPORTED = 7   /* request outside what this build supports */
+} am_status;
+
+typedef enum { AM_FP32 = 0, AM_FP64 = 1 } am_precision;
+
+/* Dealiasing of the nonlinear term.  REFERENCE reproduces cutoff_func
+ * (ActFlow_V3-2.cu:899-919) including its 32-bit overflow of the radius (every
+ * mode kept up to 256^2 and at 384^2/768^2, only k = 0 at 512^2..4096^2); HALF
+ * is the isotropic 1/2 rule (kx/kx_max)^2 + (ky/ky_max)^2 <= 1/4; NONE keeps
+ * every mode. */
+typedef enum { AM_DEALIAS_REFERENCE = 0, AM_DEALIAS_HALF = 1, AM_DEALIAS_NONE = 2 } am_dealias;
+
+/* Linear operator L(k).  REFERENCE: -(1 - k^2)^2 - alpha (lin_func,
+ * ActFlow_V3-2.cu:1030), mean-flow factor exp(-(1 + alpha) dt)
+ * (ActFlow_V3-2.cu:704).  GENERAL: -alpha - gamma0 k^2 - gamma2 k^4 with
+ * mean-flow factor exp(-alpha dt) -- the dimensional form of the same model. */
+typedef enum { AM_FORM_REFERENCE = 0, AM_FORM_GENERAL = 1 } am_form;
+
+typedef struct am_params {
+    int nx, ny;              /* grid; powers of two, 8..4096 (FP64: Ny <= 4096) */
+    double lx, ly;           /* box lengths */
+    double dt;               /* time step */
+    double lambda, alpha, beta;
+    double gamma0, gamma2;   /* AM_FORM_GENERAL only */
+    int form;                /* am_form */
+    int dealias;             /* am_dealias */
+    int precision;           /* am_precision */
+    int reserved[5];         /* must be zero */
+} am_params;
+
+typedef struct am_handle am_handle;
+
+/* Allocate device buffers, twiddle and wavenumber tables and the integrating
+ * factors for one simulation.  Replaces the reference's set-up
+ * (ActFlow_V3-2.cu:409-521: derived parameters, cudaMallocManaged of every
+ * array, cufftPlan2d, wavenumber_func, cutoff_func) and lin_func / lin_v
+ * (ActFlow_V3-2.cu:699-705). */
+am_status am_create(const am_params *p, am_handle **out);
+
+/* Free everything (unallocate_func, ActFlow_V3-2.cu:1280-1326). */
+am_status am_destroy(am_handle *h);
+
+/* Run all work of this handle on `cuda_stream` (a cudaStream_t; NULL selects
+ * the handle's own stream).  The reference runs on the default stream. */
+am_status am_set_stream(am_handle *h, void *cuda_stream);
+
+/* Load the state from host memory: w_hat [Ny][Nx/2+1] complex in the handle's
+ * precision, mean[2] scaled mean velocity.  Replaces reading a snapshot into
+ * w_new and the mean scalars (ActFlow_V3-2.cu:620-631). */
+am_status am_set_state(am_handle *h, const void *w_hat, const double mean[2]);
+
+/* Load the state from a real-space field w_real [Ny][Nx] (handle precision):
+ * forward R2C on the device, then, when `mask_and_zero_mean` is nonzero, the
+ * dealias mask and w(0,0) = 0 -- the reference's processing of a fresh initial
+ * condition (ActFlow_V3-2.cu:660-679). */
+am_status am_set_state_real(am_handle *h, const void *w_real, const double mean[2], int mask_and_zero_mean);
+
+/* Copy the state to host memory (same layout as am_set_state).  Replaces the
+ * device-to-host copy of save_func (ActFlow_V3-2.cu:1259-1263). */
+am_status am_get_state(am_handle *h, void *w_hat, double mean[2]);
+
+/* Advance nsteps integrating-factor RK4 steps (the time loop body,
+ * ActFlow_V3-2.cu:718-862).  energy, if not NULL, receives nsteps values: the
+ * energy of the state at the start of each step.  Returns AM_ERR_NAN if Re
+ * w(0,0) became NaN (check_func, ActFlow_V3-2.cu:884-897); *nan_step (if not
+ * NULL) then holds the 0-based index of that step within this call, otherwise -1. */
+am_status am_step(am_handle *h, int nsteps, double *energy, int *nan_step);
+
+/* Enqueue nsteps steps on the handle's stream and return without waiting.  The
+ * energies stay on the device; am_sync waits and reports a NaN. */
+am_status am_step_async(am_handle *h, int nsteps);
+am_status am_sync(am_handle *h);
+
+/* Advance nsteps steps launching the 8 kernels of each step individually with
+ * CUDA events between them on the handle's stream, and add each kernel's
+ * duration (milliseconds) to row_ms[stage-1] / col_ms[stage-1] (stage 1..4).
+ * For measurement; am_step is the production path (one CUDA graph per step). */
+am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double col_ms[4]);
+
+/* Number of kernel launches one step makes (for accounting). */
+int am_launches_per_step(const am_handle *h);
+
+/* Device bytes held by the handle. */
+long long am_device_bytes(const am_handle *h);
+
+/* Human-readable text for a status, and the last error detail of a handle. */
+const char *am_status_string(am_status s);
+const char *am_last_error(const am_handle *h);
+
+/* The reference's dealias mask value at half-plane index (ix, iy) (host-only,
+ * no GPU needed).  Mirrors cutoff_func (ActFlow_V3-2.cu:899-919). */
+int am_mask_value(int nx, int ny, int dealias, int ix, int iy);
+
+/* Seeded band-limited initial field (host-only, no GPU needed): modes with
+ * integer index kmin <= |(ix, iy)| <= kmax, Gaussian amplitudes and uniform
+ * phases from a 64-bit Mersenne Twister seeded with `seed`, Hermitian, zero
+ * mean, real-space rms `rms`.  Writes [Ny][Nx/2+1] complex doubles.  The
+ * reference's own random field (ActFlow_V3-2.cu:535-559) is seeded from the
+ * clock and cannot be reproduced; this generator replaces it for benchmarks. */
+am_status am_ic_bandlimited(int nx, int ny, unsigned long long seed, double kmin, double kmax, double rms,
+                            double *w_hat);
+
+/* ------------------------------------------------ host-only file boundary --
+ * These entry points need no GPU.  They are the reference program's file
+ * contract, shared by the `actflow` front end and the tests. */
+
+typedef struct am_spec {
+    double T, dt, lx, ly;    /* parsed into float, widened to double */
+    int nx, ny;
+    double lambda, alpha, beta, dt_snap;
+    double gamma0, gamma2;   /* extension keys Gamma0: / Gamma2: */
+    int has_gamma;
+    int precision;           /* extension key precision: fp32 | fp64 */
+    int dealias;             /* extension key dealias: reference | half | none */
+    char initial[256];
+    char directory[1024];
+} am_spec;
+
+/* Read <dir>/specifications.txt (ActFlow_V3-2.cu:320-408): reference defaults
+ * (ActFlow_V3-2.cu:183-204), reference keys and value parsing.  AM_ERR_IO if the
+ * file is missing, AM_ERR_SPEC for an unknown key (ActFlow_V3-2.cu:392-400) or
+ * an unreadable value; `err` receives the message. */
+am_status am_spec_read(const char *dir, am_spec *out, char *err, int errlen);
+
+/* Write a snapshot file in the reference's text layout (save_func,
+ * ActFlow_V3-2.cu:1245-1266): Ny*(Nx/2+1) pairs "re,im," then "mx,my", each in
+ * the default ostream form (%g).  w_hat is float for AM_FP32, double for AM_FP64. */
+am_status am_write_snapshot(const char *path, int nx, int ny, int precision, const void *w_hat,
+                            const double mean[2]);
+
+/* Parse a snapshot file (the continue reader, ActFlow_V3-2.cu:614-634). */
+am_status am_read_snapshot(const char *path, int nx, int ny, int precision, void *w_hat, double mean[2]);
+
+/* Append `count` energy lines "t E" for steps m0, m0+1, ... (save_energy_func,
+ * ActFlow_V3-2.cu:1268-1278); t = (float)m * dt evaluated in float. */
+am_status am_append_energy(const char *path, long long m0, int count, float dt, const double *energy, int precision);
+
+/* The whole drop-in program: `actflow <dir>` / help / spec / math
+ * (main, ActFlow_V3-2.cu:214-878).  Returns the process exit code. */
+int am_cli_main(int argc, char **argv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

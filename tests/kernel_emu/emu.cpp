@@ -1,0 +1,181 @@
+// CPU execution of the CUDA kernel bodies, for the test suite.
+//
+// The step kernels are written as host/device templates (csrc/fft.cuh,
+// csrc/step_kernels.cuh, csrc/setup_kernels.cuh).  This harness compiles them
+// with g++ and runs each CTA with one std::thread per CUDA thread and a
+// std::barrier for __syncthreads(), using exactly the launch shapes and the
+// host set-up (csrc/host_tables.h) of the CUDA build.  It checks the kernels'
+// index arithmetic, shared-memory exchange and stage logic against the oracle
+// on small grids without a GPU.  It is test code only: the product never runs
+// kernels on the CPU.
+#include <barrier>
+#include <cstring>
+#include <functional>
+#include <thread>
+#include <vector>
+
+#include "host_tables.h"
+#include "setup_kernels.cuh"
+
+using namespace af;
+
+namespace {
+
+template <class Body>
+void launch(int grid, int threads, size_t smem, Body body)
+{
+    std::vector<unsigned char> sm(smem, 0);
+    for (int b = 0; b < grid; b++) {
+        std::barrier bar(threads);
+        auto sync = [&bar]() { bar.arrive_and_wait(); };
+        std::vector<std::thread> ts;
+        ts.reserve(threads);
+        for (int t = 0; t < threads; t++) ts.emplace_back([&, t]() { body(t, b, sm.data(), sync); });
+        for (auto &th : ts) th.join();
+    }
+}
+
+template <typename T, int LX, int LY>
+struct Runner {
+    static int run(const am_params &p, T *w_hat, double *mean, int nsteps, double *energy)
+    {
+        HostTables<T> t;
+        StepArgs<T> a{};
+        host_setup<T>(p, t, a, 1 << 16);
+        const int W = Tile<T>::W, nx = p.nx, ny = p.ny;
+        const size_t fsz = (size_t)t.nt * W * ny;
+        std::vector<cpx<T>> u0(fsz), acc(fsz), fa(fsz), fx(fsz), fy(fsz), P(fsz), Q(fsz);
+        std::vector<double> rowp((size_t)ny * 3), en(1 << 16);
+        Scalars sc{};
+        a.u0 = u0.data(); a.acc = acc.data(); a.fa = fa.data(); a.fx = fx.data(); a.fy = fy.data();
+        a.P = P.data(); a.Q = Q.data(); a.twx = t.twx.data(); a.twy = t.twy.data();
+        a.kxt = t.kx.data(); a.kyt = t.ky.data(); a.rowp = rowp.data(); a.sc = &sc; a.energy = en.data();
+        // tile the input
+        for (int y = 0; y < ny; y++)
+            for (int k = 0; k < t.nxh; k++) {
+                size_t s = ((size_t)y * t.nxh + k) * 2;
+                u0[tidx<T>(k, y, ny)] = mk(w_hat[s], w_hat[s + 1]);
+            }
+        sc.m_new[0] = mean[0];
+        sc.m_new[1] = mean[1];
+        sc.nan_step = -1;
+        using RP = RowPass<T, LX>;
+        using CP = ColPass<T, LY>;
+        auto col = [&](int mode) {
+            StepArgs<T> b = a;
+            b.mode = mode;
+            launch((t.nt + CP::TILES - 1) / CP::TILES, CP::THREADS, CP::smem_bytes(),
+                   [&](int tid, int bid, unsigned char *sm, auto &sync) { CP::body(b, tid, bid, sm, sync); });
+        };
+        auto row = [&]() {
+            launch((ny + RP::ROWS - 1) / RP::ROWS, RP::THREADS, RP::smem_bytes(),
+                   [&](int tid, int bid, unsigned char *sm, auto &sync) { RP::body(a, tid, bid, sm, sync); });
+        };
+        col(0);
+        for (int m = 0; m < nsteps; m++) {
+            for (int s = 1; s <= 4; s++) {
+                row();
+                col(s);
+            }
+        }
+        for (int m = 0; m < nsteps; m++) energy[m] = en[m];
+        for (int y = 0; y < ny; y++)
+            for (int k = 0; k < t.nxh; k++) {
+                size_t s = ((size_t)y * t.nxh + k) * 2;
+                cpx<T> v = u0[tidx<T>(k, y, ny)];
+                w_hat[s] = v.x;
+                w_hat[s + 1] = v.y;
+            }
+        mean[0] = sc.m_new[0];
+        mean[1] = sc.m_new[1];
+        (void)nx;
+        return sc.nan_step;
+    }
+
+    static void forward(const am_params &p, const T *real, T *w_hat, int mask)
+    {
+        HostTables<T> t;
+        StepArgs<T> a{};
+        host_setup<T>(p, t, a, 16);
+        const int W = Tile<T>::W, ny = p.ny;
+        const size_t fsz = (size_t)t.nt * W * ny;
+        std::vector<cpx<T>> mid(fsz), out(fsz);
+        using RF = RowFwd<T, LX>;
+        using CF = ColFwd<T, LY>;
+        launch((ny + RF::ROWS - 1) / RF::ROWS, RF::THREADS, RF::smem_bytes(),
+               [&](int tid, int bid, unsigned char *sm, auto &sync) {
+                   RF::body(real, mid.data(), t.twx.data(), ny, t.nt, tid, bid, sm, sync);
+               });
+        launch((t.nt + CF::TILES - 1) / CF::TILES, CF::THREADS, CF::smem_bytes(),
+               [&](int tid, int bid, unsigned char *sm, auto &sync) {
+                   CF::body(mid.data(), out.data(), t.twy.data(), p.nx, ny, t.nxh, t.nt, mask, p.dealias,
+                            a.rsq, tid, bid, sm, sync);
+               });
+        for (int y = 0; y < ny; y++)
+            for (int k = 0; k < t.nxh; k++) {
+                size_t s = ((size_t)y * t.nxh + k) * 2;
+                cpx<T> v = out[tidx<T>(k, y, ny)];
+                w_hat[s] = v.x;
+                w_hat[s + 1] = v.y;
+            }
+    }
+};
+
+template <typename T, int LX, int LY>
+int dispatch_y(const am_params &p, T *w, double *m, int n, double *e, const T *real, int fwd, int mask)
+{
+    if (fwd) {
+        Runner<T, LX, LY>::forward(p, real, w, mask);
+        return 0;
+    }
+    return Runner<T, LX, LY>::run(p, w, m, n, e);
+}
+
+template <typename T, int LX>
+int dispatch_x(int ly, const am_params &p, T *w, double *m, int n, double *e, const T *real, int fwd, int mask)
+{
+    switch (ly) {
+    case 3: return dispatch_y<T, LX, 3>(p, w, m, n, e, real, fwd, mask);
+    case 4: return dispatch_y<T, LX, 4>(p, w, m, n, e, real, fwd, mask);
+    case 5: return dispatch_y<T, LX, 5>(p, w, m, n, e, real, fwd, mask);
+    case 6: return dispatch_y<T, LX, 6>(p, w, m, n, e, real, fwd, mask);
+    case 7: return dispatch_y<T, LX, 7>(p, w, m, n, e, real, fwd, mask);
+    }
+    return -100;
+}
+
+template <typename T>
+int dispatch(const am_params &p, T *w, double *m, int n, double *e, const T *real, int fwd, int mask)
+{
+    int lx = 0, ly = 0;
+    while ((1 << lx) < p.nx) lx++;
+    while ((1 << ly) < p.ny) ly++;
+    switch (lx) {
+    case 3: return dispatch_x<T, 3>(ly, p, w, m, n, e, real, fwd, mask);
+    case 4: return dispatch_x<T, 4>(ly, p, w, m, n, e, real, fwd, mask);
+    case 5: return dispatch_x<T, 5>(ly, p, w, m, n, e, real, fwd, mask);
+    case 6: return dispatch_x<T, 6>(ly, p, w, m, n, e, real, fwd, mask);
+    case 7: return dispatch_x<T, 7>(ly, p, w, m, n, e, real, fwd, mask);
+    }
+    return -100;
+}
+
+}  // namespace
+
+extern "C" {
+// Advance (w_hat [ny][nx/2+1] complex of the precision, mean[2]) nsteps steps.
+// Returns the first NaN step or -1; -100 for an unsupported size (8..128).
+int emu_run(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy)
+{
+    if (p->precision == AM_FP64)
+        return dispatch<double>(*p, (double *)w_hat, mean, nsteps, energy, nullptr, 0, 0);
+    return dispatch<float>(*p, (float *)w_hat, mean, nsteps, energy, nullptr, 0, 0);
+}
+
+int emu_forward(const am_params *p, const void *real, void *w_hat, int mask)
+{
+    if (p->precision == AM_FP64)
+        return dispatch<double>(*p, (double *)w_hat, nullptr, 0, nullptr, (const double *)real, 1, mask);
+    return dispatch<float>(*p, (float *)w_hat, nullptr, 0, nullptr, (const float *)real, 1, mask);
+}
+}

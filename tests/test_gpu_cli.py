@@ -1,0 +1,102 @@
+"""The drop-in program on the GPU: `actflow <dir>` against the reference's own
+outputs for the same specifications.txt (process contract of ActFlow_V3-2.cu:
+exit codes, energy.txt, ActTurb_snap{i}.bin)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from refformat import read_energy, read_snapshot, write_snapshot_exact, write_spec
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _run(am, d):
+    exe = am.CLI_PATH
+    return subprocess.run([exe, d], capture_output=True, text=True, timeout=600)
+
+
+def test_cli_reference_example_1024(am, tmp_path):
+    """The shipped example spec (1024^2, random 42): the reference writes
+    energy.txt = '0.005 0\\n0.01 0\\n' and an all-zero snapshot 0."""
+    d = str(tmp_path)
+    write_spec(os.path.join(d, "specifications.txt"), [
+        ("T", "0.01"), ("dt", "0.005"), ("Lx", "628.3185307"), ("Ly", "628.3185307"),
+        ("Nx", 1024), ("Ny", 1024), ("alpha", "-0.8"), ("beta", "0.01"), ("lambda", "7"),
+        ("dt_snap", "1000"), ("initial_condition", "random 42"), ("save_directory", d)])
+    p = _run(am, d)
+    assert p.returncode == 0, p.stderr
+    gold = np.load(os.path.join(GOLD, "example1024.npz"))
+    with open(os.path.join(d, "energy.txt")) as f:
+        assert f.read() == str(gold["energy_txt"])
+    w, m = read_snapshot(os.path.join(d, "ActTurb_snap0.bin"), 1024, 1024)
+    assert np.abs(w).max() == 0.0 and np.all(m == 0)
+
+
+@pytest.mark.parametrize("name", ["format8", "small64"])
+def test_cli_continue_matches_reference_outputs(am, tmp_path, name):
+    """Same injected field, same spec: snapshots and energy.txt agree with the
+    reference's files to its six printed digits."""
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+    nx, ny, dt, steps, snap = int(g["nx"]), int(g["ny"]), float(g["dt"]), int(g["steps"]), int(g["snap"])
+    d = str(tmp_path)
+    write_spec(os.path.join(d, "specifications.txt"), [
+        ("T", "%.9g" % ((steps - 1) * dt)), ("dt", "%.9g" % dt), ("Lx", "%.9g" % float(g["lx"])),
+        ("Ly", "%.9g" % float(g["ly"])), ("Nx", nx), ("Ny", ny), ("lambda", "%.9g" % float(g["lam"])),
+        ("alpha", "%.9g" % float(g["alpha"])), ("beta", "%.9g" % float(g["beta"])),
+        ("dt_snap", "%.9g" % (snap * dt)), ("initial_condition", "continue"), ("save_directory", d)])
+    write_snapshot_exact(os.path.join(d, "ActTurb_snap0.bin"), g["w0"], g["mean0"])
+    p = _run(am, d)
+    assert p.returncode == 0, p.stderr
+    t, e = read_energy(os.path.join(d, "energy.txt"))
+    assert len(e) == steps
+    assert np.allclose(t, g["energy_t"], rtol=1e-6, atol=0)
+    assert np.abs(e - g["energy"]).max() <= 1e-5 * np.abs(g["energy"]).max()
+    idx = sorted(int(k[4:]) for k in g.keys() if k.startswith("snap") and k[4:].isdigit())
+    for i in idx:
+        w, m = read_snapshot(os.path.join(d, f"ActTurb_snap{i}.bin"), nx, ny)
+        ref = g[f"snap{i}"]
+        assert np.linalg.norm(w - ref) / np.linalg.norm(ref) < 5e-6
+    if name == "format8":
+        # Same number of fields and separators as the reference's files.
+        for i in idx:
+            with open(os.path.join(GOLD, f"format8_snap{i}.txt")) as f:
+                ref_txt = f.read()
+            with open(os.path.join(d, f"ActTurb_snap{i}.bin")) as f:
+                txt = f.read()
+            assert txt.count(",") == ref_txt.count(",") and not txt.endswith(",")
+
+
+def test_cli_nan_exits_1(am, tmp_path):
+    d = str(tmp_path)
+    nx = ny = 16
+    write_spec(os.path.join(d, "specifications.txt"), [
+        ("T", "0.05"), ("dt", "0.01"), ("Lx", "20"), ("Ly", "20"), ("Nx", nx), ("Ny", ny),
+        ("dt_snap", "0.02"), ("initial_condition", "continue"), ("save_directory", d)])
+    w = np.zeros((ny, nx // 2 + 1), np.complex64)
+    w[0, 0] = np.nan
+    write_snapshot_exact(os.path.join(d, "ActTurb_snap0.bin"), w, (0.0, 0.0))
+    p = _run(am, d)
+    assert p.returncode == 1
+    assert "nan values after 0 timesteps" in p.stderr
+    # the reference writes the energy of step 0 and snapshot 0 (0 % snap == 0)
+    t, e = read_energy(os.path.join(d, "energy.txt"))
+    assert len(t) == 1
+
+
+def test_cli_fresh_bandlimited_fp64(am, tmp_path):
+    d = str(tmp_path)
+    write_spec(os.path.join(d, "specifications.txt"), [
+        ("T", "0.01"), ("dt", "0.001"), ("Lx", "6.283185307"), ("Ly", "6.283185307"), ("Nx", 64), ("Ny", 64),
+        ("lambda", "3.5"), ("alpha", "-0.8"), ("beta", "0.01"), ("dt_snap", "0.005"),
+        ("initial_condition", "bandlimited 42"), ("save_directory", d), ("precision", "fp64"),
+        ("dealias", "half"), ("Gamma0", "-0.045"), ("Gamma2", "2.5e-5")])
+    p = _run(am, d)
+    assert p.returncode == 0, p.stderr
+    t, e = read_energy(os.path.join(d, "energy.txt"))
+    assert len(t) == 10 and abs(t[0] - 0.001) < 1e-9
+    assert os.path.exists(os.path.join(d, "ActTurb_snap2.bin"))

@@ -1,0 +1,84 @@
+"""The CUDA kernel bodies executed on the CPU (tests/kernel_emu/emu.cpp: one
+std::thread per CUDA thread, std::barrier for __syncthreads) against the
+oracle.  Checks index arithmetic, shared-memory exchanges and the fused stage
+logic without a GPU; the GPU tests then check the compiled kernels."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+EMU_DIR = os.path.join(ROOT, "tests", "kernel_emu")
+EMU_LIB = os.path.join(EMU_DIR, "_build", "libemu.so")
+GOLD = os.path.join(ROOT, "tests", "golden")
+
+
+@pytest.fixture(scope="session")
+def emu(am):
+    src = os.path.join(EMU_DIR, "emu.cpp")
+    csrc = os.path.join(ROOT, "2d_active_matter_simulation_gb300", "csrc")
+    deps = [src] + [os.path.join(csrc, f) for f in os.listdir(csrc) if f.endswith((".cuh", ".h"))]
+    if not os.path.exists(EMU_LIB) or any(os.path.getmtime(d) > os.path.getmtime(EMU_LIB) for d in deps):
+        os.makedirs(os.path.dirname(EMU_LIB), exist_ok=True)
+        subprocess.run(["g++", "-std=c++20", "-O2", "-pthread", "-shared", "-fPIC", "-ffp-contract=off",
+                        "-I" + os.path.join(ROOT, "include"), "-I" + csrc, src, "-o", EMU_LIB], check=True)
+    L = ctypes.CDLL(EMU_LIB)
+    L.emu_run.argtypes = [ctypes.POINTER(am.Params), ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                          ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    L.emu_forward.argtypes = [ctypes.POINTER(am.Params), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    return L
+
+
+def _emu_run(am, emu, p, w0, mean0, n):
+    w = np.ascontiguousarray(w0, dtype=np.complex128 if p.precision else np.complex64).copy()
+    m = np.array(mean0, dtype=np.float64)
+    e = np.zeros(max(n, 1))
+    r = emu.emu_run(ctypes.byref(p), w.ctypes.data, m.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n,
+                    e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert r == -1
+    return w, m, e[:n]
+
+
+@pytest.mark.parametrize("name", ["format8", "small64", "rect64x32", "rect32x64"])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_emulated_kernels_match_oracle(am, orc, emu, name, prec):
+    d = np.load(os.path.join(GOLD, name + ".npz"))
+    nx, ny = int(d["nx"]), int(d["ny"])
+    p = am.Params(nx, ny, float(d["lx"]), float(d["ly"]), float(d["dt"]), float(d["lam"]), float(d["alpha"]),
+                  float(d["beta"]), 0.0, 0.0, 0, 0, prec)
+    w, m, e = _emu_run(am, emu, p, d["w0"], d["mean0"], 3)
+    op = orc.make_params(nx, ny, float(d["lx"]), float(d["ly"]), float(d["dt"]), float(d["lam"]),
+                         float(d["alpha"]), float(d["beta"]))
+    wo, mo, eo = orc.run(op, d["w0"], d["mean0"], 3, "f64")
+    tol = 1e-13 if prec else 1e-6
+    assert np.linalg.norm(w - wo) / np.linalg.norm(wo) < tol
+    assert np.abs(m - mo).max() <= tol * np.abs(mo).max()
+    assert np.abs(e - eo).max() <= tol * np.abs(eo).max()
+
+
+@pytest.mark.parametrize("dealias", ["reference", "half", "none"])
+def test_emulated_general_form_and_masks(am, orc, emu, dealias):
+    nx, ny = 128, 64
+    w0 = am.ic_bandlimited(nx, ny, seed=9, kmax=10.0, rms=3.0)
+    p = am.Params(nx, ny, 6.283185307179586, 3.141592653589793, 1e-3, 3.5, -0.8, 0.01, -0.045, 2.5e-5, 1,
+                  am.DEALIAS[dealias], 1)
+    w, m, e = _emu_run(am, emu, p, w0, (50.0, -20.0), 2)
+    op = orc.make_params(nx, ny, 6.283185307179586, 3.141592653589793, 1e-3, 3.5, -0.8, 0.01, -0.045, 2.5e-5,
+                         dealias=dealias)
+    wo, mo, eo = orc.run(op, w0, (50.0, -20.0), 2, "f64")
+    assert np.linalg.norm(w - wo) / np.linalg.norm(wo) < 1e-13
+    assert np.abs(m - mo).max() <= 1e-13 * np.abs(mo).max()
+
+
+@pytest.mark.parametrize("n", [(8, 8), (64, 32), (16, 128), (128, 128)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_emulated_forward_transform(am, emu, n, prec):
+    nx, ny = n
+    p = am.Params(nx, ny, 1.0, 1.0, 0.1, 1.0, 1.0, 1.0, 0.0, 0.0, 0, 2, prec)
+    x = np.random.default_rng(nx * ny).standard_normal((ny, nx)).astype(np.float64 if prec else np.float32)
+    w = np.zeros((ny, nx // 2 + 1), np.complex128 if prec else np.complex64)
+    emu.emu_forward(ctypes.byref(p), x.ctypes.data, w.ctypes.data, 0)
+    ref = np.fft.rfft2(x.astype(np.float64))
+    assert np.abs(w - ref).max() <= (1e-14 if prec else 5e-7) * np.abs(ref).max()

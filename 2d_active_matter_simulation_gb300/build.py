@@ -58,6 +58,18 @@ def _run(cmd):
 
 def build(verbose=False):
     os.makedirs(OBJ, exist_ok=True)
+    # Objects built on another machine type (the tree is shared between an
+    # x86-64 build host and aarch64 GPU hosts) are discarded.
+    import platform
+    stamp = os.path.join(LIB, "BUILD_ARCH")
+    arch = platform.machine()
+    prev = open(stamp).read().strip() if os.path.exists(stamp) else None
+    if prev != arch:
+        for f in glob.glob(os.path.join(OBJ, "*.o")) + [os.path.join(LIB, "libactflow.so"), os.path.join(LIB, "actflow")]:
+            if os.path.exists(f):
+                os.remove(f)
+        with open(stamp, "w") as fh:
+            fh.write(arch + "\n")
     hdrs = _headers()
     jobs = []
     for u in CUDA_UNITS:

@@ -149,7 +149,11 @@ static am_status alloc_and_tables(am_handle *h)
         const void *fn;
         size_t smem;
     } ks[] = {{(const void *)K.row[h->lognx], K.row_shape[h->lognx].smem},
-              {(const void *)K.col[h->logny], K.col_shape[h->logny].smem},
+              {(const void *)K.col[h->logny][0], K.col_shape[h->logny].smem},
+              {(const void *)K.col[h->logny][1], K.col_shape[h->logny].smem},
+              {(const void *)K.col[h->logny][2], K.col_shape[h->logny].smem},
+              {(const void *)K.col[h->logny][3], K.col_shape[h->logny].smem},
+              {(const void *)K.col[h->logny][4], K.col_shape[h->logny].smem},
               {(const void *)K.rowfwd[h->lognx], K.rowfwd_shape[h->lognx].smem},
               {(const void *)K.colfwd[h->logny], K.colfwd_shape[h->logny].smem}};
     for (auto &k : ks) {
@@ -167,7 +171,7 @@ static am_status launch_col(am_handle *h, int mode)
     a.mode = mode;
     const LaunchShape &s = K.col_shape[h->logny];
     int grid = (h->nt + s.per_block - 1) / s.per_block;
-    K.col[h->logny]<<<grid, s.threads, s.smem, h->stream>>>(a);
+    K.col[h->logny][mode]<<<grid, s.threads, s.smem, h->stream>>>(a);
     CK(h, cudaGetLastError());
     return AM_OK;
 }

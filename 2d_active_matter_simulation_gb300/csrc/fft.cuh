@@ -128,30 +128,31 @@ struct DFT {
 };
 
 // Shared-memory exchange buffer for W interleaved transforms (W columns of a
-// tile, or W = 1 for a single row).  Real and imaginary parts live in separate
-// arrays; element idx of transform c sits at word PAD(idx) * W + c.  The padding
-// functions were chosen by simulating the bank pattern of every pass.
-template <typename T, int W, int PADK>
+// tile, or W = 1 for a single row).  Complex values are stored whole (one
+// 8- or 16-byte access each); element idx of transform c sits at slot
+// SWZ(idx) * W + c.  The index maps were chosen by simulating the bank pattern of
+// every pass of the transforms that use them (vector accesses are served per
+// half- or quarter-warp):
+//   SWZ 0: idx + idx/8          column passes (W = 4 FP32, W = 2 FP64)
+//   SWZ 1: idx ^ ((idx/16) % 16) row passes, FP32 (a permutation: no padding)
+//   SWZ 2: idx + idx/4          row passes, FP64
+template <typename T, int W, int SWZ>
 struct XBuf {
-    T *re, *im;
+    cpx<T> *d;
     AF_HDC static constexpr int pad(int i)
     {
-        if constexpr (PADK == 36) return i + (i >> 3) + (i >> 6);
-        else return i + (i >> PADK);
+        if constexpr (SWZ == 0) return i + (i >> 3);
+        else if constexpr (SWZ == 1) return i ^ ((i >> 4) & 15);
+        else return i + (i >> 2);
     }
-    AF_HDC static constexpr int words(int L) { return pad(L - 1) * W + W; }
-    AF_HD int w(int idx, int c) const { return pad(idx) * W + c; }
-    AF_HD void put(int idx, int c, cpx<T> v) const
+    // slots needed for L elements
+    AF_HDC static constexpr int slots(int L)
     {
-        int k = w(idx, c);
-        re[k] = v.x;
-        im[k] = v.y;
+        if constexpr (SWZ == 1) return (L < 16 ? 16 : L) * W;
+        else return pad(L - 1) * W + W;
     }
-    AF_HD cpx<T> get(int idx, int c) const
-    {
-        int k = w(idx, c);
-        return mk(re[k], im[k]);
-    }
+    AF_HD void put(int idx, int c, cpx<T> v) const { d[pad(idx) * W + c] = v; }
+    AF_HD cpx<T> get(int idx, int c) const { return d[pad(idx) * W + c]; }
 };
 
 // Twiddle source: tw[m * STRIDE] = exp(-2 pi i m / L) for m < L.
@@ -178,6 +179,33 @@ AF_HD cpx<double> ldtw(const cpx<double> *tw, int idx)
 // L/R threads.  `sync` is the block barrier (called identically by every
 // thread of the block).  tw must hold exp(-2 pi i m / (L * TWS)) at index m for
 // m < L * TWS; the transform uses every TWS-th entry.
+// Twiddle powers w[r] = W^{r k} (r = 1..R-1) for one pass, from the table
+// entry at r * step.  FP32: the powers 1, 2, 4, 8 are loaded and the others
+// formed by at most three complex products (error a few ulp); FP64: all loaded.
+template <int R, typename T>
+AF_HD void twiddles(cpx<T> *w, const cpx<T> *tw, int step)
+{
+    if constexpr (sizeof(T) == 8 || R <= 2) {
+#pragma unroll
+        for (int r = 1; r < R; r++) w[r] = ldtw(tw, r * step);
+    } else {
+        w[1] = ldtw(tw, step);
+        w[2] = ldtw(tw, 2 * step);
+        w[3] = cmul(w[2], w[1]);
+        if constexpr (R >= 8) {
+            w[4] = ldtw(tw, 4 * step);
+            w[5] = cmul(w[4], w[1]);
+            w[6] = cmul(w[4], w[2]);
+            w[7] = cmul(w[4], w[3]);
+        }
+        if constexpr (R >= 16) {
+            w[8] = ldtw(tw, 8 * step);
+#pragma unroll
+            for (int r = 9; r < 16; r++) w[r] = cmul(w[8], w[r - 8]);
+        }
+    }
+}
+
 template <typename T, int LOGL, int LOGR_MAX, int SIGN>
 struct BlockFFT {
     static constexpr int LOGR = LOGR_MAX < LOGL ? LOGR_MAX : LOGL;
@@ -225,11 +253,10 @@ struct BlockFFT {
             if (Ns > 1) {
                 int k = j & (Ns - 1);
                 int step = (L / (Ns * R)) * k * TWS;   // twiddle index of W^{k}
+                cpx<T> w[R];
+                twiddles<R>(w, tw, step);
 #pragma unroll
-                for (int r = 1; r < R; r++) {
-                    cpx<T> w = ldtw(tw, r * step);
-                    v[r] = SIGN < 0 ? cmul(v[r], w) : cmulc(v[r], w);
-                }
+                for (int r = 1; r < R; r++) v[r] = SIGN < 0 ? cmul(v[r], w[r]) : cmulc(v[r], w[r]);
             }
             DFT<R, SIGN, T>::run(v);
             if (p < NPASS - 1) {

@@ -21,7 +21,7 @@ template <typename T>
 struct KernelTable {
     void (*row[LOG_MAX + 1])(StepArgs<T>);
     LaunchShape row_shape[LOG_MAX + 1];
-    void (*col[LOG_MAX + 1])(StepArgs<T>);
+    void (*col[LOG_MAX + 1][5])(StepArgs<T>);   // [log2 Ny][mode]
     LaunchShape col_shape[LOG_MAX + 1];
     void (*rowfwd[LOG_MAX + 1])(const T *, cpx<T> *, const cpx<T> *, int, int);
     LaunchShape rowfwd_shape[LOG_MAX + 1];

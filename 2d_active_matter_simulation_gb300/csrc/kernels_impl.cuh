@@ -7,17 +7,17 @@
 namespace af {
 
 template <typename T, int LOG>
-__global__ void __launch_bounds__(RowPass<T, LOG>::THREADS) k_row(StepArgs<T> a)
+__global__ void __launch_bounds__(RowPass<T, LOG>::THREADS, RowPass<T, LOG>::MINB) k_row(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     RowPass<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
-template <typename T, int LOG>
-__global__ void __launch_bounds__(ColPass<T, LOG>::THREADS) k_col(StepArgs<T> a)
+template <typename T, int LOG, int MODE>
+__global__ void __launch_bounds__(ColPass<T, LOG, MODE>::THREADS) k_col(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    ColPass<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+    ColPass<T, LOG, MODE>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
 template <typename T, int LOG>
@@ -70,8 +70,12 @@ struct Fill {
     {
         t.row[LOG] = k_row<T, LOG>;
         t.row_shape[LOG] = {RowPass<T, LOG>::THREADS, RowPass<T, LOG>::smem_bytes(), RowPass<T, LOG>::ROWS};
-        t.col[LOG] = k_col<T, LOG>;
-        t.col_shape[LOG] = {ColPass<T, LOG>::THREADS, ColPass<T, LOG>::smem_bytes(), ColPass<T, LOG>::TILES};
+        t.col[LOG][0] = k_col<T, LOG, 0>;
+        t.col[LOG][1] = k_col<T, LOG, 1>;
+        t.col[LOG][2] = k_col<T, LOG, 2>;
+        t.col[LOG][3] = k_col<T, LOG, 3>;
+        t.col[LOG][4] = k_col<T, LOG, 4>;
+        t.col_shape[LOG] = {ColPass<T, LOG, 1>::THREADS, ColPass<T, LOG, 1>::smem_bytes(), ColPass<T, LOG, 1>::TILES};
         t.rowfwd[LOG] = k_rowfwd<T, LOG>;
         t.rowfwd_shape[LOG] = {RowFwd<T, LOG>::THREADS, RowFwd<T, LOG>::smem_bytes(), RowFwd<T, LOG>::ROWS};
         t.colfwd[LOG] = k_colfwd<T, LOG>;

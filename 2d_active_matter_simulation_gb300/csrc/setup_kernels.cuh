@@ -13,45 +13,41 @@ namespace af {
 template <typename T, int LOGNX>
 struct RowFwd {
     using RP = RowPass<T, LOGNX>;
-    static constexpr int M = RP::M, LOGM = RP::LOGM, R = RP::R, TPC = RP::TPC;
-    static constexpr int ROWS = RP::ROWS, THREADS = RP::THREADS, BUFW = RP::BUFW;
+    static constexpr int M = RP::M, R = RP::R, TPC = RP::TPC;
+    static constexpr int ROWS = RP::ROWS, THREADS = RP::THREADS, BUFS = RP::BUFS;
     using Buf = typename RP::Buf;
     using FFTf = typename RP::FFTf;
-    static constexpr size_t smem_bytes() { return (size_t)ROWS * 2 * BUFW * sizeof(T); }
+    static constexpr size_t smem_bytes() { return RP::smem_bytes(); }
 
     template <class Sync>
     static AF_HD void body(const T *src, cpx<T> *dst, const cpx<T> *twx, int ny, int nt, int tid, int bid,
                            unsigned char *smem, Sync &&sync)
     {
         const int rl = tid / TPC, j = tid % TPC;
-        const int y = bid * ROWS + rl;
-        const bool active = y < ny;
+        const int yy = bid * ROWS + rl;
+        const bool active = yy < ny;
+        const int y = active ? yy : ny - 1;
         const int nx = 2 * M;
-        T *base = reinterpret_cast<T *>(smem);
-        Buf buf{base + (size_t)rl * 2 * BUFW, base + (size_t)rl * 2 * BUFW + BUFW};
+        Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * BUFS};
         cpx<T> v[R];
 #pragma unroll
         for (int r = 0; r < R; r++) {
             int n = j + r * TPC;
-            v[r] = active ? mk(src[(size_t)y * nx + 2 * n], src[(size_t)y * nx + 2 * n + 1]) : mk<T>(0, 0);
+            v[r] = mk(src[(size_t)y * nx + 2 * n], src[(size_t)y * nx + 2 * n + 1]);
         }
         FFTf::run(v, j, 0, buf, twx, 2, sync);
         sync();
 #pragma unroll
         for (int r = 0; r < R; r++) buf.put(j + r * TPC, 0, v[r]);
         sync();
-        const int kend = nt * Tile<T>::W;
-        for (int kx = j; kx < kend; kx += TPC) {
-            cpx<T> X = mk<T>(0, 0);
-            if (kx <= M) {
-                cpx<T> A = buf.get(kx & (M - 1), 0);
-                cpx<T> B = conj(buf.get((M - kx) & (M - 1), 0));
-                cpx<T> E = scale(A + B, (T)0.5);
-                cpx<T> D = scale(A - B, (T)0.5);
-                X = E + cmul(mk(D.y, -D.x), ldtw(twx, kx));
-            }
-            if (active) dst[tidx<T>(kx, y, ny)] = X;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            int k = j + r * TPC;
+            cpx<T> X = RP::unpack(v[r], buf.get((M - k) & (M - 1), 0), ldtw(twx, k));
+            if (active) dst[tidx<T>(k, y, ny)] = X;
         }
+        if (active && j == 0) dst[tidx<T>(M, y, ny)] = RP::unpack(v[0], v[0], mk<T>(-1, 0));
+        for (int kx = M + 1 + j; active && kx < nt * Tile<T>::W; kx += TPC) dst[tidx<T>(kx, y, ny)] = mk<T>(0, 0);
     }
 };
 
@@ -60,12 +56,12 @@ struct RowFwd {
 // w(0,0) set to zero (ActFlow_V3-2.cu:679).
 template <typename T, int LOGNY>
 struct ColFwd {
-    using CP = ColPass<T, LOGNY>;
+    using CP = ColPass<T, LOGNY, 0>;
     static constexpr int W = CP::W, R = CP::R, TPC = CP::TPC, TILES = CP::TILES, THREADS = CP::THREADS;
-    static constexpr int BUFW = CP::BUFW;
+    static constexpr int BUFS = CP::BUFS;
     using Buf = typename CP::Buf;
     using FFTf = typename CP::FFTf;
-    static constexpr size_t smem_bytes() { return (size_t)TILES * 2 * BUFW * sizeof(T); }
+    static constexpr size_t smem_bytes() { return (size_t)TILES * BUFS * sizeof(cpx<T>); }
 
     template <class Sync>
     static AF_HD void body(const cpx<T> *src, cpx<T> *dst, const cpx<T> *twy, int nx, int ny, int nxh, int nt,
@@ -77,8 +73,7 @@ struct ColFwd {
         const int tile = bid * TILES + tl;
         const bool active = tile < nt;
         const int kx = tile * W + c;
-        T *base = reinterpret_cast<T *>(smem);
-        Buf buf{base + (size_t)tl * 2 * BUFW, base + (size_t)tl * 2 * BUFW + BUFW};
+        Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)tl * BUFS};
         const size_t cbase = active ? (size_t)tile * ny * W + c : 0;
         cpx<T> v[R];
 #pragma unroll

@@ -101,141 +101,155 @@ AF_HD float expT(float x) { return expf(x); }
 AF_HD double expT(double x) { return exp(x); }
 
 // ------------------------------------------------------------------ row pass
+// One row y per group of TPC threads; a complex FFT of length M = Nx/2 per
+// real transform (the half-length real-FFT construction).  The Hermitian pairs
+// X(k), X(M-k) of the C2R inputs are read straight from global memory (the
+// partner read is a reversed but coalesced access), so the inputs are never
+// staged in shared memory.  The forward transforms pair Z(k) with Z(M-k)
+// through one shared-memory exchange.
 // Launch: blockDim = ROWS * TPC, gridDim = ceil(Ny / ROWS).
 template <typename T, int LOGNX>
 struct RowPass {
-    static constexpr int M = 1 << (LOGNX - 1);   // complex length of the half-size FFT
+    static constexpr int M = 1 << (LOGNX - 1);
     static constexpr int LOGM = LOGNX - 1;
-    static constexpr int LOGR = sizeof(T) == 4 ? 3 : 3;
+    static constexpr int LOGR = 3;
     using FFTi = BlockFFT<T, LOGM, LOGR, +1>;
     using FFTf = BlockFFT<T, LOGM, LOGR, -1>;
     static constexpr int R = FFTi::R;
     static constexpr int TPC = FFTi::TPC;
-    static constexpr int ROWS = TPC >= 256 ? 1 : 256 / TPC;
+    static constexpr int ROWS = TPC >= 128 ? 1 : 128 / TPC;
     static constexpr int THREADS = ROWS * TPC;
-    using Buf = XBuf<T, 1, 4>;
-    static constexpr int BUFW = (Buf::words(M + 1) + 31) / 32 * 32;   // words per row buffer
+    static constexpr int MINB = sizeof(T) == 4 ? 4 : 2;   // resident CTAs per SM (register cap)
+    using Buf = XBuf<T, 1, sizeof(T) == 4 ? 1 : 2>;
+    static constexpr int BUFS = (Buf::slots(M) + 7) / 8 * 8;   // complex slots per row
 
-    static constexpr size_t smem_bytes()
+    static constexpr size_t smem_bytes() { return (size_t)ROWS * BUFS * sizeof(cpx<T>); }
+
+    // C2R pre-processing of X(k), X(M-k): Z(k) = E + i O with
+    // E = X(k) + conj X(M-k), O = (X(k) - conj X(M-k)) exp(2 pi i k / Nx).
+    static AF_HD cpx<T> pack(const cpx<T> *src, int k, int y, int ny, const cpx<T> *twx)
     {
-        return (size_t)ROWS * 2 * BUFW * sizeof(T) + (size_t)ROWS * TPC * 3 * sizeof(double);
+        cpx<T> A = src[tidx<T>(k, y, ny)];
+        cpx<T> B = src[tidx<T>(M - k, y, ny)];
+        if (k == 0) {   // X(0), X(M): imaginary parts dropped, as a half-plane C2R does
+            A.y = 0;
+            B.y = 0;
+        }
+        B.y = -B.y;
+        cpx<T> E = A + B;
+        cpx<T> O = cmulc(A - B, ldtw(twx, k));
+        return mk(E.x - O.y, E.y + O.x);
+    }
+
+    // R2C post-processing: X(k) = E + exp(-2 pi i k / Nx) O with
+    // E = (Z(k) + conj Z(M-k)) / 2, O = (Z(k) - conj Z(M-k)) / (2i).
+    static AF_HD cpx<T> unpack(cpx<T> A, cpx<T> Bp, cpx<T> w)
+    {
+        cpx<T> B = conj(Bp);
+        cpx<T> E = scale(A + B, (T)0.5);
+        cpx<T> D = scale(A - B, (T)0.5);
+        return E + cmul(mk(D.y, -D.x), w);
     }
 
     template <class Sync>
     static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync)
     {
         const int rl = tid / TPC, j = tid % TPC;
-        const int y = bid * ROWS + rl;
-        const bool active = y < a.ny;
+        const int yy = bid * ROWS + rl;
+        const bool active = yy < a.ny;
+        const int y = active ? yy : a.ny - 1;   // inactive rows recompute the last row, never store
         const int ny = a.ny;
-        T *base = reinterpret_cast<T *>(smem);
-        Buf buf{base + (size_t)rl * 2 * BUFW, base + (size_t)rl * 2 * BUFW + BUFW};
-        double *red = reinterpret_cast<double *>(base + (size_t)ROWS * 2 * BUFW) + (size_t)rl * TPC * 3;
+        Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * BUFS};
 
-        cpx<T> z[3][R];
-        const cpx<T> *src[3] = {a.fx, a.fy, a.fa};
+        // ---- C2R along x of uy, ux (kept) and w (consumed by the products)
+        cpx<T> zy[R], zx[R], v[R];
 #pragma unroll
-        for (int f = 0; f < 3; f++) {
-            sync();
-            // Stage X(kx, y), kx = 0..M; the imaginary parts at kx = 0 and kx = M
-            // are dropped, as a half-plane C2R does.
-            for (int kx = j; kx <= M; kx += TPC) {
-                cpx<T> v = mk<T>(0, 0);
-                if (active) v = src[f][tidx<T>(kx, y, ny)];
-                if (kx == 0 || kx == M) v.y = 0;
-                buf.put(kx, 0, v);
-            }
-            sync();
-            // Pack the Hermitian half spectrum into a length-M complex spectrum:
-            // Z(k) = E(k) + i O(k), E = X(k) + conj X(M-k),
-            // O = (X(k) - conj X(M-k)) * exp(+2 pi i k / Nx).
-            cpx<T> v[R];
+        for (int r = 0; r < R; r++) v[r] = pack(a.fy, j + r * TPC, y, ny, a.twx);
+        FFTi::run(v, j, 0, buf, a.twx, 2, sync);
 #pragma unroll
-            for (int r = 0; r < R; r++) {
-                int k = j + r * TPC;
-                cpx<T> A = buf.get(k, 0);
-                cpx<T> B = conj(buf.get(M - k, 0));
-                cpx<T> E = A + B;
-                cpx<T> O = cmulc(A - B, ldtw(a.twx, k));
-                v[r] = mk(E.x - O.y, E.y + O.x);
-            }
-            FFTi::run(v, j, 0, buf, a.twx, 2, sync);
+        for (int r = 0; r < R; r++) zy[r] = v[r];
 #pragma unroll
-            for (int r = 0; r < R; r++) z[f][r] = v[r];
-        }
+        for (int r = 0; r < R; r++) v[r] = pack(a.fx, j + r * TPC, y, ny, a.twx);
+        FFTi::run(v, j, 0, buf, a.twx, 2, sync);
+#pragma unroll
+        for (int r = 0; r < R; r++) zx[r] = v[r];
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = pack(a.fa, j + r * TPC, y, ny, a.twx);
+        FFTi::run(v, j, 0, buf, a.twx, 2, sync);
 
-        // Real-space products and per-thread partial sums.  z[.][r] holds the
-        // real values at x = 2n (real part) and x = 2n + 1 (imaginary part),
-        // n = j + r * TPC.  Order: 0 = ux, 1 = uy, 2 = w.
+        // ---- real-space products; z[r] holds x = 2n (real part) and 2n + 1
+        // (imaginary part), n = j + r * TPC.  P overwrites zx, Q overwrites zy.
         T se = 0, sx = 0, sy = 0;
-        cpx<T> p[R], q[R];
         const T lam = a.lam_s, bet = a.beta_s;
 #pragma unroll
         for (int r = 0; r < R; r++) {
-            T ux0 = z[0][r].x, uy0 = z[1][r].x, w0 = z[2][r].x;
-            T ux1 = z[0][r].y, uy1 = z[1][r].y, w1 = z[2][r].y;
+            T ux0 = zx[r].x, uy0 = zy[r].x, w0 = v[r].x;
+            T ux1 = zx[r].y, uy1 = zy[r].y, w1 = v[r].y;
             T s0 = ux0 * ux0 + uy0 * uy0, s1 = ux1 * ux1 + uy1 * uy1;
             se += s0 + s1;
             sx += s0 * ux0 + s1 * ux1;
             sy += s0 * uy0 + s1 * uy1;
-            p[r] = mk(lam * w0 * ux0 + bet * s0 * uy0, lam * w1 * ux1 + bet * s1 * uy1);
-            q[r] = mk(lam * w0 * uy0 - bet * s0 * ux0, lam * w1 * uy1 - bet * s1 * ux1);
+            zx[r] = mk(lam * w0 * ux0 + bet * s0 * uy0, lam * w1 * ux1 + bet * s1 * uy1);
+            zy[r] = mk(lam * w0 * uy0 - bet * s0 * ux0, lam * w1 * uy1 - bet * s1 * ux1);
         }
 
-        // Row sums: tree reduction in double over the TPC threads of the row.
-        sync();
-        red[j] = (double)se;
-        red[TPC + j] = (double)sx;
-        red[2 * TPC + j] = (double)sy;
-        sync();
-        for (int s = TPC / 2; s > 0; s >>= 1) {
-            if (j < s) {
-                red[j] += red[j + s];
-                red[TPC + j] += red[TPC + j + s];
-                red[2 * TPC + j] += red[2 * TPC + j + s];
-            }
+        // ---- row sums (double tree over the row's TPC threads; the exchange
+        // buffer doubles as scratch)
+        {
+            double *red = reinterpret_cast<double *>(buf.d);
             sync();
-        }
-        if (active && j == 0) {
-            a.rowp[(size_t)y * 3 + 0] = red[0];
-            a.rowp[(size_t)y * 3 + 1] = red[TPC];
-            a.rowp[(size_t)y * 3 + 2] = red[2 * TPC];
+            red[j] = (double)se;
+            red[TPC + j] = (double)sx;
+            red[2 * TPC + j] = (double)sy;
+            sync();
+            for (int s = TPC / 2; s > 0; s >>= 1) {
+                if (j < s) {
+                    red[j] += red[j + s];
+                    red[TPC + j] += red[TPC + j + s];
+                    red[2 * TPC + j] += red[2 * TPC + j + s];
+                }
+                sync();
+            }
+            if (active && j == 0) {
+                a.rowp[(size_t)y * 3 + 0] = red[0];
+                a.rowp[(size_t)y * 3 + 1] = red[TPC];
+                a.rowp[(size_t)y * 3 + 2] = red[2 * TPC];
+            }
         }
 
-        // Forward R2C along x of P and Q.
+        // ---- R2C along x of P and Q
 #pragma unroll
         for (int f = 0; f < 2; f++) {
-            cpx<T> v[R];
 #pragma unroll
-            for (int r = 0; r < R; r++) v[r] = f == 0 ? p[r] : q[r];
+            for (int r = 0; r < R; r++) v[r] = f == 0 ? zx[r] : zy[r];
             FFTf::run(v, j, 0, buf, a.twx, 2, sync);
             sync();
 #pragma unroll
             for (int r = 0; r < R; r++) buf.put(j + r * TPC, 0, v[r]);
             sync();
-            // Unpack: X(k) = E(k) + exp(-2 pi i k / Nx) O(k) with
-            // E = (Z(k) + conj Z(M-k)) / 2, O = (Z(k) - conj Z(M-k)) / (2i).
             cpx<T> *dst = f == 0 ? a.P : a.Q;
-            const int kend = a.nt * Tile<T>::W;
-            for (int kx = j; kx < kend; kx += TPC) {
-                cpx<T> X = mk<T>(0, 0);
-                if (kx <= M) {
-                    cpx<T> A = buf.get(kx & (M - 1), 0);
-                    cpx<T> B = conj(buf.get((M - kx) & (M - 1), 0));
-                    cpx<T> E = scale(A + B, (T)0.5);
-                    cpx<T> D = scale(A - B, (T)0.5);
-                    cpx<T> O = mk(D.y, -D.x);
-                    X = E + cmul(O, ldtw(a.twx, kx));
-                }
-                if (active) dst[tidx<T>(kx, y, ny)] = X;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                int k = j + r * TPC;
+                cpx<T> X = unpack(v[r], buf.get((M - k) & (M - 1), 0), ldtw(a.twx, k));
+                if (active) dst[tidx<T>(k, y, ny)] = X;
             }
+            if (active && j == 0) {   // kx = M: E(0) - O(0)
+                cpx<T> X = unpack(v[0], v[0], mk<T>(-1, 0));
+                dst[tidx<T>(M, y, ny)] = X;
+            }
+            for (int kx = M + 1 + j; active && kx < a.nt * Tile<T>::W; kx += TPC) dst[tidx<T>(kx, y, ny)] = mk<T>(0, 0);
         }
     }
 };
 
 // --------------------------------------------------------------- column pass
+// One tile of W adjacent kx columns per group of W * TPC threads (lane c =
+// column inside the tile, j = thread of that column's transform), so every
+// warp access to the tile is one contiguous block.  MODE 0 starts from u0
+// (after set_state), MODE 1..4 is the RK stage.
 // Launch: blockDim = TILES * W * TPC, gridDim = ceil(nt / TILES).
-template <typename T, int LOGNY>
+template <typename T, int LOGNY, int MODE>
 struct ColPass {
     static constexpr int W = Tile<T>::W;
     static constexpr int LOGR = sizeof(T) == 4 ? 4 : 3;
@@ -246,14 +260,10 @@ struct ColPass {
     static constexpr int L = 1 << LOGNY;
     static constexpr int TILES = W * TPC >= 128 ? 1 : 128 / (W * TPC);
     static constexpr int THREADS = TILES * W * TPC;
-    static constexpr int PADK = sizeof(T) == 4 ? 36 : 4;
-    using Buf = XBuf<T, W, PADK>;
-    static constexpr int BUFW = (Buf::words(L) + 31) / 32 * 32;
+    using Buf = XBuf<T, W, 0>;
+    static constexpr int BUFS = (Buf::slots(L) + 7) / 8 * 8;
 
-    static constexpr size_t smem_bytes()
-    {
-        return (size_t)TILES * 2 * BUFW * sizeof(T) + (size_t)THREADS * 3 * sizeof(double) + 8 * sizeof(double);
-    }
+    static constexpr size_t smem_bytes() { return (size_t)TILES * BUFS * sizeof(cpx<T>) + 8 * sizeof(double); }
 
     template <class Sync>
     static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync)
@@ -266,18 +276,17 @@ struct ColPass {
         const int kx = tile * W + c;
         const bool col = active && kx < a.nxh;   // a real (non-padding) column
         const int ny = a.ny, nx = a.nx;
-        const int mode = a.mode;
-        T *base = reinterpret_cast<T *>(smem);
-        Buf buf{base + (size_t)tl * 2 * BUFW, base + (size_t)tl * 2 * BUFW + BUFW};
-        double *red = reinterpret_cast<double *>(base + (size_t)TILES * 2 * BUFW);
-        double *bc = red + (size_t)THREADS * 3;   // broadcast slots
-        const bool owner = bid == 0;              // this CTA holds column kx = 0
+        Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)tl * BUFS};
+        double *red = reinterpret_cast<double *>(smem);   // owner-CTA scratch, aliases the buffers
+        double *bc = reinterpret_cast<double *>(smem + (size_t)TILES * BUFS * sizeof(cpx<T>));
+        const bool owner = bid == 0;   // this CTA holds column kx = 0
         const T kxv = active ? a.kxt[kx] : (T)0;
         const size_t cbase = active ? (size_t)tile * ny * W + c : 0;
+        const T dt = a.dt;
 
-        // ---- forward FFT along y of P and Q, assembly of N = i(-kx P^ - ky Q^) * mask
+        // ---- forward FFT along y of P and Q, N = i (-kx P^ - ky Q^) * mask
         cpx<T> nl[R];
-        if (mode != 0) {
+        if constexpr (MODE != 0) {
             cpx<T> ph[R], v[R];
 #pragma unroll
             for (int r = 0; r < R; r++) v[r] = active ? a.P[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
@@ -301,7 +310,7 @@ struct ColPass {
         // ---- mean flow and energy: reduce the row sums (CTA holding kx = 0)
         if (owner) {
             double se = 0, sx = 0, sy = 0;
-            if (mode != 0) {
+            if constexpr (MODE != 0) {
                 for (int y = tid; y < ny; y += THREADS) {
                     se += a.rowp[(size_t)y * 3 + 0];
                     sx += a.rowp[(size_t)y * 3 + 1];
@@ -313,133 +322,122 @@ struct ColPass {
             red[THREADS + tid] = sx;
             red[2 * THREADS + tid] = sy;
             sync();
+            for (int s = THREADS / 2; s > 0; s >>= 1) {
+                if (tid < s) {
+                    red[tid] += red[tid + s];
+                    red[THREADS + tid] += red[THREADS + tid + s];
+                    red[2 * THREADS + tid] += red[2 * THREADS + tid + s];
+                }
+                sync();
+            }
             if (tid == 0) {
                 Scalars *s = a.sc;
-                double Se = 0, Sx = 0, Sy = 0;
-                for (int t = 0; t < THREADS; t++) {
-                    Se += red[t];
-                    Sx += red[THREADS + t];
-                    Sy += red[2 * THREADS + t];
-                }
                 // Mean-flow right-hand side -beta' Re F[|u|^2 u](0)
                 // (ActFlow_V3-2.cu:1086-1087) and its stage updates
                 // (ActFlow_V3-2.cu:729-732, 756-759, 778-781, 799-802, 820-821).
-                double n0 = -a.beta_sd * Sx, n1 = -a.beta_sd * Sy;
-                const double dt = (double)a.dt;
-                if (mode == 0) {
-                    for (int d = 0; d < 2; d++) {
-                        s->m_old[d] = s->m_new[d];
-                        s->m_appr[d] = s->m_new[d];
-                    }
-                } else if (mode == 1) {
-                    a.energy[s->step % a.ecap] = Se * a.inv_2n3;
-                    s->m_new[0] += dt / 6 * a.lin_v * n0;
-                    s->m_new[1] += dt / 6 * a.lin_v * n1;
-                    s->m_appr[0] = a.lin2_v * (s->m_old[0] + dt / 2 * n0);
-                    s->m_appr[1] = a.lin2_v * (s->m_old[1] + dt / 2 * n1);
-                } else if (mode == 2) {
-                    s->m_new[0] += dt / 3 * a.lin2_v * n0;
-                    s->m_new[1] += dt / 3 * a.lin2_v * n1;
-                    s->m_appr[0] = a.lin2_v * (s->m_old[0] + dt / 2 * n0);
-                    s->m_appr[1] = a.lin2_v * (s->m_old[1] + dt / 2 * n1);
-                } else if (mode == 3) {
-                    s->m_new[0] += dt / 3 * a.lin2_v * n0;
-                    s->m_new[1] += dt / 3 * a.lin2_v * n1;
-                    s->m_appr[0] = a.lin_v * (s->m_old[0] + dt * n0);
-                    s->m_appr[1] = a.lin_v * (s->m_old[1] + dt * n1);
+                const double n0 = -a.beta_sd * red[THREADS], n1 = -a.beta_sd * red[2 * THREADS];
+                const double dd = (double)dt;
+                if constexpr (MODE == 0) {
+                    for (int d = 0; d < 2; d++) s->m_old[d] = s->m_appr[d] = s->m_new[d];
+                } else if constexpr (MODE == 1) {
+                    a.energy[s->step % a.ecap] = red[0] * a.inv_2n3;
+                    s->m_new[0] += dd / 6 * a.lin_v * n0;
+                    s->m_new[1] += dd / 6 * a.lin_v * n1;
+                    s->m_appr[0] = a.lin2_v * (s->m_old[0] + dd / 2 * n0);
+                    s->m_appr[1] = a.lin2_v * (s->m_old[1] + dd / 2 * n1);
+                } else if constexpr (MODE == 2) {
+                    s->m_new[0] += dd / 3 * a.lin2_v * n0;
+                    s->m_new[1] += dd / 3 * a.lin2_v * n1;
+                    s->m_appr[0] = a.lin2_v * (s->m_old[0] + dd / 2 * n0);
+                    s->m_appr[1] = a.lin2_v * (s->m_old[1] + dd / 2 * n1);
+                } else if constexpr (MODE == 3) {
+                    s->m_new[0] += dd / 3 * a.lin2_v * n0;
+                    s->m_new[1] += dd / 3 * a.lin2_v * n1;
+                    s->m_appr[0] = a.lin_v * (s->m_old[0] + dd * n0);
+                    s->m_appr[1] = a.lin_v * (s->m_old[1] + dd * n1);
                 } else {
-                    s->m_new[0] += dt / 6 * n0;
-                    s->m_new[1] += dt / 6 * n1;
-                    for (int d = 0; d < 2; d++) {
-                        s->m_old[d] = s->m_new[d];
-                        s->m_appr[d] = s->m_new[d];
-                    }
+                    s->m_new[0] += dd / 6 * n0;
+                    s->m_new[1] += dd / 6 * n1;
+                    for (int d = 0; d < 2; d++) s->m_old[d] = s->m_appr[d] = s->m_new[d];
                 }
                 bc[0] = s->m_appr[0];
                 bc[1] = s->m_appr[1];
             }
+            sync();
         }
 
         // ---- RK stage combination (integrate_func_0..4, ActFlow_V3-2.cu:940-1018)
-        // with the Hermitian repair of the accumulator's kx = 0 column before
-        // the addition (reality_func, ActFlow_V3-2.cu:1228-1243).
+        // with the Hermitian repair of the accumulator's kx = 0 column before the
+        // addition (reality_func, ActFlow_V3-2.cu:1228-1243).
         cpx<T> av[R];
-        {
+        if constexpr (MODE == 0) {
+#pragma unroll
+            for (int r = 0; r < R; r++) av[r] = active ? a.u0[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
+        } else {
             cpx<T> accv[R];
-            T E[R], E2[R];
-            const T dt = a.dt;
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                int iy = j + r * TPC;
-                T kyv = a.kyt[iy];
-                T k2 = kyv * kyv + kxv * kxv;
-                T Lk = a.form == 0 ? -(1 - k2) * (1 - k2) - a.alpha : -a.alpha - a.g0 * k2 - a.g2 * k2 * k2;
-                E[r] = expT(Lk * dt);
-                E2[r] = expT(Lk * dt / 2);
-                size_t g = cbase + (size_t)iy * W;
-                if (mode == 0) {
-                    av[r] = active ? a.u0[g] : mk<T>(0, 0);
-                } else if (mode == 1) {
-                    cpx<T> u = active ? a.u0[g] : mk<T>(0, 0);
-                    av[r] = u;                      // keep u0 for the stage input
-                    accv[r] = scale(u, E[r]);       // w_new = w_old * lin
+                size_t g = cbase + (size_t)(j + r * TPC) * W;
+                if constexpr (MODE == 1) {
+                    av[r] = active ? a.u0[g] : mk<T>(0, 0);   // w_old
+                    accv[r] = scale(av[r], lin_at(a, kxv, j + r * TPC, dt));   // w_new = w_old * lin
                 } else {
                     accv[r] = active ? a.acc[g] : mk<T>(0, 0);
+                    if constexpr (MODE != 4) av[r] = active ? a.u0[g] : mk<T>(0, 0);
                 }
             }
-            if (mode != 0) {
-                if (owner) {
-                    sync();
-                    if (tl == 0 && c == 0) {
+            if (owner) {
+                sync();
+                if (tl == 0 && c == 0) {
 #pragma unroll
-                        for (int r = 0; r < R; r++) buf.put(j + r * TPC, 0, accv[r]);
-                    }
-                    sync();
-                    if (tl == 0 && c == 0) {
+                    for (int r = 0; r < R; r++) buf.put(j + r * TPC, 0, accv[r]);
+                }
+                sync();
+                if (tl == 0 && c == 0) {
 #pragma unroll
-                        for (int r = 0; r < R; r++) {
-                            int iy = j + r * TPC;
-                            if (iy >= 1 && iy < ny / 2) {
-                                cpx<T> b = buf.get(ny - iy, 0);
-                                accv[r] = mk((T)0.5f * (accv[r].x + b.x), (T)0.5f * (accv[r].y - b.y));
-                            } else if (iy > ny / 2) {
-                                cpx<T> b = buf.get(ny - iy, 0);
-                                cpx<T> m = mk((T)0.5f * (b.x + accv[r].x), (T)0.5f * (b.y - accv[r].y));
-                                accv[r] = conj(m);
-                            }
+                    for (int r = 0; r < R; r++) {
+                        int iy = j + r * TPC;
+                        if (iy >= 1 && iy < ny / 2) {
+                            cpx<T> b = buf.get(ny - iy, 0);
+                            accv[r] = mk((T)0.5f * (accv[r].x + b.x), (T)0.5f * (accv[r].y - b.y));
+                        } else if (iy > ny / 2) {
+                            cpx<T> b = buf.get(ny - iy, 0);
+                            accv[r] = conj(mk((T)0.5f * (b.x + accv[r].x), (T)0.5f * (b.y - accv[r].y)));
                         }
                     }
                 }
-                if (mode != 1) {
+            }
 #pragma unroll
-                    for (int r = 0; r < R; r++) av[r] = active ? a.u0[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
+            for (int r = 0; r < R; r++) {
+                const int iy = j + r * TPC;
+                const size_t g = cbase + (size_t)iy * W;
+                const cpx<T> n = nl[r], o = av[r];
+                cpx<T> w = accv[r];
+                if constexpr (MODE == 1) {
+                    T e2 = lin_at(a, kxv, iy, dt / 2);
+                    T f = dt / 6 * lin_at(a, kxv, iy, dt);
+                    w = mk(w.x + f * n.x, w.y + f * n.y);
+                    av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), e2);
+                } else if constexpr (MODE == 2) {
+                    T e2 = lin_at(a, kxv, iy, dt / 2);
+                    T f = dt / 3 * e2;
+                    w = mk(w.x + f * n.x, w.y + f * n.y);
+                    av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), e2);
+                } else if constexpr (MODE == 3) {
+                    T f = dt / 3 * lin_at(a, kxv, iy, dt / 2);
+                    w = mk(w.x + f * n.x, w.y + f * n.y);
+                    av[r] = scale(mk(o.x + dt * n.x, o.y + dt * n.y), lin_at(a, kxv, iy, dt));
+                } else {
+                    w = mk(w.x + dt / 6 * n.x, w.y + dt / 6 * n.y);
+                    av[r] = w;   // next step: w_old = w_appr = w_new
                 }
-#pragma unroll
-                for (int r = 0; r < R; r++) {
-                    cpx<T> n = nl[r], o = av[r], w = accv[r];
-                    size_t g = cbase + (size_t)(j + r * TPC) * W;
-                    if (mode == 1) {
-                        T f = dt / 6 * E[r];
-                        w = mk(w.x + f * n.x, w.y + f * n.y);
-                        av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), E2[r]);
-                    } else if (mode == 2) {
-                        T f = dt / 3 * E2[r];
-                        w = mk(w.x + f * n.x, w.y + f * n.y);
-                        av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), E2[r]);
-                    } else if (mode == 3) {
-                        T f = dt / 3 * E2[r];
-                        w = mk(w.x + f * n.x, w.y + f * n.y);
-                        av[r] = scale(mk(o.x + dt * n.x, o.y + dt * n.y), E[r]);
-                    } else {
-                        w = mk(w.x + dt / 6 * n.x, w.y + dt / 6 * n.y);
-                        av[r] = w;                  // next step: w_old = w_appr = w_new
-                    }
-                    if (active) {
-                        if (mode == 4) a.u0[g] = w;
-                        else a.acc[g] = w;
-                    }
+                if (active) {
+                    if constexpr (MODE == 4) a.u0[g] = w;
+                    else a.acc[g] = w;
                 }
-                if (mode == 4 && owner && tid == 0) {
+            }
+            if constexpr (MODE == 4) {
+                if (owner && tid == 0) {
                     // NaN probe on Re w(0,0) (check_func, ActFlow_V3-2.cu:884-897).
                     Scalars *s = a.sc;
                     if (av[0].x != av[0].x && s->nan_step < 0) s->nan_step = s->step;
@@ -451,27 +449,25 @@ struct ColPass {
         // ---- Biot-Savart (nonl_subfunc_0, ActFlow_V3-2.cu:1176-1180) and the
         // mean velocity in the k = 0 slot (ActFlow_V3-2.cu:1053-1054), then the
         // inverse FFT along y of a, ux, uy.
-        if (owner) sync();   // bc[] written by thread 0 above
         T m0 = 0, m1 = 0;
         if (owner) {
             m0 = (T)bc[0];
             m1 = (T)bc[1];
         }
-#pragma unroll
+#pragma unroll 1
         for (int f = 0; f < 3; f++) {
             cpx<T> v[R];
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                int iy = j + r * TPC;
-                cpx<T> w = av[r];
+                const int iy = j + r * TPC;
+                const cpx<T> w = av[r];
                 if (f == 0) {
                     v[r] = col ? w : mk<T>(0, 0);
                 } else {
-                    T kyv = a.kyt[iy];
-                    T k2 = kyv * kyv + kxv * kxv;
-                    T kk = f == 1 ? kyv : -kxv;
-                    cpx<T> iw = mk(-w.y, w.x);
-                    v[r] = (col && (kx != 0 || iy != 0)) ? mk(iw.x * kk / k2, iw.y * kk / k2) : mk<T>(0, 0);
+                    const T kyv = a.kyt[iy];
+                    const T k2 = kyv * kyv + kxv * kxv;
+                    const T kk = f == 1 ? kyv : -kxv;
+                    v[r] = (col && (kx != 0 || iy != 0)) ? mk(-w.y * kk / k2, w.x * kk / k2) : mk<T>(0, 0);
                     if (owner && kx == 0 && iy == 0) v[r] = mk(f == 1 ? m0 : m1, (T)0);
                 }
             }
@@ -482,6 +478,16 @@ struct ColPass {
                 for (int r = 0; r < R; r++) dst[cbase + (size_t)(j + r * TPC) * W] = v[r];
             }
         }
+    }
+
+    // exp(L(k) h) at (kx, ky index iy): L = -(1 - k^2)^2 - alpha (lin_func,
+    // ActFlow_V3-2.cu:1030) or -alpha - g0 k^2 - g2 k^4, evaluated in T.
+    static AF_HD T lin_at(const StepArgs<T> &a, T kxv, int iy, T h)
+    {
+        T kyv = a.kyt[iy];
+        T k2 = kyv * kyv + kxv * kxv;
+        T Lk = a.form == 0 ? -(1 - k2) * (1 - k2) - a.alpha : -a.alpha - a.g0 * k2 - a.g2 * k2 * k2;
+        return expT(Lk * h);
     }
 };
 

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <functional>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "host_tables.h"
@@ -60,12 +61,19 @@ struct Runner {
         sc.m_new[1] = mean[1];
         sc.nan_step = -1;
         using RP = RowPass<T, LX>;
-        using CP = ColPass<T, LY>;
         auto col = [&](int mode) {
-            StepArgs<T> b = a;
-            b.mode = mode;
-            launch((t.nt + CP::TILES - 1) / CP::TILES, CP::THREADS, CP::smem_bytes(),
-                   [&](int tid, int bid, unsigned char *sm, auto &sync) { CP::body(b, tid, bid, sm, sync); });
+            auto go = [&](auto tag) {
+                using CP = ColPass<T, LY, decltype(tag)::value>;
+                launch((t.nt + CP::TILES - 1) / CP::TILES, CP::THREADS, CP::smem_bytes(),
+                       [&](int tid, int bid, unsigned char *sm, auto &sync) { CP::body(a, tid, bid, sm, sync); });
+            };
+            switch (mode) {
+            case 0: go(std::integral_constant<int, 0>{}); break;
+            case 1: go(std::integral_constant<int, 1>{}); break;
+            case 2: go(std::integral_constant<int, 2>{}); break;
+            case 3: go(std::integral_constant<int, 3>{}); break;
+            default: go(std::integral_constant<int, 4>{}); break;
+            }
         };
         auto row = [&]() {
             launch((ny + RP::ROWS - 1) / RP::ROWS, RP::THREADS, RP::smem_bytes(),

@@ -170,7 +170,7 @@ static am_status launch_col(am_handle *h, int mode)
     StepArgs<T> a = args_of<T>(h);
     a.mode = mode;
     const LaunchShape &s = K.col_shape[h->logny];
-    int grid = (h->nt + s.per_block - 1) / s.per_block;
+    int grid = (a.ntp + s.per_block - 1) / s.per_block;
     K.col[h->logny][mode]<<<grid, s.threads, s.smem, h->stream>>>(a);
     CK(h, cudaGetLastError());
     return AM_OK;
@@ -229,9 +229,25 @@ static am_status reset_scalars(am_handle *h, const double mean[2])
     return AM_OK;
 }
 
+// Select pruned transforms when the 1/2 rule is on and the state is zero
+// outside its ellipse; the step graph bakes the launch shape in, so it is
+// rebuilt when the choice changes.
+template <typename T>
+static void choose_pruning(am_handle *h, bool on)
+{
+    StepArgs<T> &a = args_of<T>(h);
+    const int old = a.ntp;
+    set_pruning<T>(a, on && h->p.dealias == AM_DEALIAS_HALF);
+    if (a.ntp != old && h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+}
+
 template <typename T>
 static am_status set_state_impl(am_handle *h, const void *w_hat, const double mean[2])
 {
+    choose_pruning<T>(h, state_inside_half_mask<T>((const T *)w_hat, h->p.nx, h->p.ny));
     const size_t bytes = (size_t)h->p.ny * h->nxh * sizeof(cpx<T>);
     CK(h, cudaMemcpyAsync(h->stage, w_hat, bytes, cudaMemcpyHostToDevice, h->stream));
     table<T>().tile<<<1024, 256, 0, h->stream>>>((const cpx<T> *)h->stage, (cpx<T> *)h->u0, h->p.ny, h->nxh,
@@ -249,6 +265,7 @@ static am_status set_state_impl(am_handle *h, const void *w_hat, const double me
 template <typename T>
 static am_status set_state_real_impl(am_handle *h, const void *w_real, const double mean[2], int mask)
 {
+    choose_pruning<T>(h, mask != 0);
     const KernelTable<T> &K = table<T>();
     const size_t bytes = (size_t)h->p.ny * h->p.nx * sizeof(T);
     CK(h, cudaMemcpyAsync(h->stage, w_real, bytes, cudaMemcpyHostToDevice, h->stream));

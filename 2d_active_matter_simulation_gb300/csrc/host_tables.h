@@ -61,6 +61,8 @@ void host_setup(const am_params &p, HostTables<T> &t, StepArgs<T> &a, int ecap)
     a.ny = ny;
     a.nxh = t.nxh;
     a.nt = t.nt;
+    a.kxp = t.nxh - 1;
+    a.ntp = t.nt;
     a.ecap = ecap;
     // FFT normalisation folded into lambda and beta in T, as the reference does
     // (ActFlow_V3-2.cu:434-436): lambda / N^2, beta / N^3.
@@ -83,6 +85,41 @@ void host_setup(const am_params &p, HostTables<T> &t, StepArgs<T> &a, int ecap)
     a.lin2_v = std::exp(L0 * p.dt / 2);
     a.inv_2n3 = 1.0 / (2.0 * nd * nd * nd);
     a.mode = 0;
+}
+
+// Pruned transforms.  Under the 1/2 rule every nonlinear term vanishes outside
+// the ellipse (kx/(Nx/2))^2 + (ky/(Ny/2))^2 <= 1/4, and the integrating factor
+// maps zero to zero, so a state that is zero outside the ellipse stays zero
+// there.  The stage fields then carry no data for kx > Nx/4: the column pass
+// skips those tiles and the row pass neither loads nor stores them.  The results
+// are those of the full transforms (the skipped entries are exact zeros).
+template <typename T>
+void set_pruning(StepArgs<T> &a, bool on)
+{
+    const int W = Tile<T>::W;
+    if (on) {
+        a.kxp = a.nx / 4;
+        a.ntp = a.kxp / W + 1;
+    } else {
+        a.kxp = a.nxh - 1;
+        a.ntp = a.nt;
+    }
+}
+
+// True if the half-plane state w ([ny][nxh] complex, interleaved) is zero at
+// every mode the 1/2 rule removes.
+template <typename T>
+bool state_inside_half_mask(const T *w, int nx, int ny)
+{
+    const int nxh = nx / 2 + 1;
+    for (int iy = 0; iy < ny; iy++) {
+        for (int ix = 0; ix < nxh; ix++) {
+            if (mask_at(1, 0, nx, ny, ix, iy)) continue;
+            size_t k = ((size_t)iy * nxh + ix) * 2;
+            if (w[k] != 0 || w[k + 1] != 0) return false;
+        }
+    }
+    return true;
 }
 
 }  // namespace af

@@ -44,6 +44,9 @@ struct Scalars {
 template <typename T>
 struct StepArgs {
     int nx, ny, nxh, nt;            // grid; nt = number of column tiles
+    int kxp, ntp;                   // highest kx carried by the stage fields and the
+                                    // number of column tiles the passes touch (pruned
+                                    // transforms: kxp = Nx/4 under the 1/2 rule)
     cpx<T> *u0, *acc;               // spectral state (kx, ky): w_old / w_new
     cpx<T> *fa, *fx, *fy;           // stage input a, ux, uy in (kx, y)
     cpx<T> *P, *Q;                  // products in (kx, y)
@@ -97,6 +100,31 @@ AF_HD int mask_at(int dealias, int rsq, int nx, int ny, int ix, int iy)
     return 1;
 }
 
+// The mask along one column ix, with the per-column part precomputed: the
+// 1/2 rule keeps ky^2 <= floor((Nx^2 Ny^2 - 16 ix^2 Ny^2) / (16 Nx^2)), exactly
+// the integer condition of mask_at; the reference mask keeps ix^2 + iy^2 <= rsq
+// or ix^2 + (Ny - iy)^2 <= rsq.
+struct ColMask {
+    int mode, ny, ix2, lim;
+    AF_HD ColMask(int dealias, int rsq, int nx, int ny_, int ix) : mode(dealias), ny(ny_), ix2(ix * ix), lim(rsq)
+    {
+        if (dealias == 1) {
+            long long X = ix, NX = nx, NY = ny_;
+            long long num = NX * NX * NY * NY - 16 * X * X * NY * NY;
+            lim = num < 0 ? -1 : (int)(num / (16 * NX * NX));
+        }
+    }
+    AF_HD bool keep(int iy) const
+    {
+        if (mode == 1) {
+            int ky = iy <= ny / 2 ? iy : iy - ny;
+            return ky * ky <= lim;
+        }
+        if (mode == 0) return ix2 + iy * iy <= lim || ix2 + (ny - iy) * (ny - iy) <= lim;
+        return true;
+    }
+};
+
 AF_HD float expT(float x) { return expf(x); }
 AF_HD double expT(double x) { return exp(x); }
 
@@ -127,10 +155,11 @@ struct RowPass {
 
     // C2R pre-processing of X(k), X(M-k): Z(k) = E + i O with
     // E = X(k) + conj X(M-k), O = (X(k) - conj X(M-k)) exp(2 pi i k / Nx).
-    static AF_HD cpx<T> pack(const cpx<T> *src, int k, int y, int ny, const cpx<T> *twx)
+    static AF_HD cpx<T> pack(const cpx<T> *src, int k, int y, int ny, int kxp, const cpx<T> *twx)
     {
-        cpx<T> A = src[tidx<T>(k, y, ny)];
-        cpx<T> B = src[tidx<T>(M - k, y, ny)];
+        // entries above kxp are zero by construction (pruned transforms) and are not read
+        cpx<T> A = k <= kxp ? src[tidx<T>(k, y, ny)] : mk<T>(0, 0);
+        cpx<T> B = M - k <= kxp ? src[tidx<T>(M - k, y, ny)] : mk<T>(0, 0);
         if (k == 0) {   // X(0), X(M): imaginary parts dropped, as a half-plane C2R does
             A.y = 0;
             B.y = 0;
@@ -164,17 +193,17 @@ struct RowPass {
         // ---- C2R along x of uy, ux (kept) and w (consumed by the products)
         cpx<T> zy[R], zx[R], v[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) v[r] = pack(a.fy, j + r * TPC, y, ny, a.twx);
+        for (int r = 0; r < R; r++) v[r] = pack(a.fy, j + r * TPC, y, ny, a.kxp, a.twx);
         FFTi::run(v, j, 0, buf, a.twx, 2, sync);
 #pragma unroll
         for (int r = 0; r < R; r++) zy[r] = v[r];
 #pragma unroll
-        for (int r = 0; r < R; r++) v[r] = pack(a.fx, j + r * TPC, y, ny, a.twx);
+        for (int r = 0; r < R; r++) v[r] = pack(a.fx, j + r * TPC, y, ny, a.kxp, a.twx);
         FFTi::run(v, j, 0, buf, a.twx, 2, sync);
 #pragma unroll
         for (int r = 0; r < R; r++) zx[r] = v[r];
 #pragma unroll
-        for (int r = 0; r < R; r++) v[r] = pack(a.fa, j + r * TPC, y, ny, a.twx);
+        for (int r = 0; r < R; r++) v[r] = pack(a.fa, j + r * TPC, y, ny, a.kxp, a.twx);
         FFTi::run(v, j, 0, buf, a.twx, 2, sync);
 
         // ---- real-space products; z[r] holds x = 2n (real part) and 2n + 1
@@ -228,17 +257,16 @@ struct RowPass {
             for (int r = 0; r < R; r++) buf.put(j + r * TPC, 0, v[r]);
             sync();
             cpx<T> *dst = f == 0 ? a.P : a.Q;
+            const int kend = a.ntp * Tile<T>::W;   // the column pass reads kx < kend
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 int k = j + r * TPC;
-                cpx<T> X = unpack(v[r], buf.get((M - k) & (M - 1), 0), ldtw(a.twx, k));
-                if (active) dst[tidx<T>(k, y, ny)] = X;
+                if (active && k < kend) dst[tidx<T>(k, y, ny)] = unpack(v[r], buf.get((M - k) & (M - 1), 0), ldtw(a.twx, k));
             }
-            if (active && j == 0) {   // kx = M: E(0) - O(0)
-                cpx<T> X = unpack(v[0], v[0], mk<T>(-1, 0));
-                dst[tidx<T>(M, y, ny)] = X;
+            if (active && j == 0 && M < kend) {   // kx = M: E(0) - O(0)
+                dst[tidx<T>(M, y, ny)] = unpack(v[0], v[0], mk<T>(-1, 0));
             }
-            for (int kx = M + 1 + j; active && kx < a.nt * Tile<T>::W; kx += TPC) dst[tidx<T>(kx, y, ny)] = mk<T>(0, 0);
+            for (int kx = M + 1 + j; active && kx < kend; kx += TPC) dst[tidx<T>(kx, y, ny)] = mk<T>(0, 0);
         }
     }
 };
@@ -272,9 +300,9 @@ struct ColPass {
         const int rem = tid % (W * TPC);
         const int c = rem % W, j = rem / W;
         const int tile = bid * TILES + tl;
-        const bool active = tile < a.nt;
+        const bool active = tile < a.ntp;
         const int kx = tile * W + c;
-        const bool col = active && kx < a.nxh;   // a real (non-padding) column
+        const bool col = active && kx <= a.kxp;   // a column that carries data
         const int ny = a.ny, nx = a.nx;
         Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)tl * BUFS};
         double *red = reinterpret_cast<double *>(smem);   // owner-CTA scratch, aliases the buffers
@@ -296,13 +324,14 @@ struct ColPass {
 #pragma unroll
             for (int r = 0; r < R; r++) v[r] = active ? a.Q[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
             FFTf::run(v, j, c, buf, a.twy, 1, sync);
+            const ColMask cm(a.dealias, a.rsq, nx, ny, kx);
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 int iy = j + r * TPC;
                 T kyv = a.kyt[iy];
                 T tr = -kxv * ph[r].x - kyv * v[r].x;
                 T ti = -kxv * ph[r].y - kyv * v[r].y;
-                T m = (col && mask_at(a.dealias, a.rsq, nx, ny, kx, iy)) ? (T)1 : (T)0;
+                T m = (col && cm.keep(iy)) ? (T)1 : (T)0;
                 nl[r] = mk(-ti * m, tr * m);
             }
         }
@@ -380,7 +409,8 @@ struct ColPass {
                 size_t g = cbase + (size_t)(j + r * TPC) * W;
                 if constexpr (MODE == 1) {
                     av[r] = active ? a.u0[g] : mk<T>(0, 0);   // w_old
-                    accv[r] = scale(av[r], lin_at(a, kxv, j + r * TPC, dt));   // w_new = w_old * lin
+                    T e2 = lin_at(a, kxv, j + r * TPC, dt / 2);
+                    accv[r] = scale(av[r], e2 * e2);          // w_new = w_old * lin
                 } else {
                     accv[r] = active ? a.acc[g] : mk<T>(0, 0);
                     if constexpr (MODE != 4) av[r] = active ? a.u0[g] : mk<T>(0, 0);
@@ -413,9 +443,10 @@ struct ColPass {
                 const size_t g = cbase + (size_t)iy * W;
                 const cpx<T> n = nl[r], o = av[r];
                 cpx<T> w = accv[r];
+                // exp(L dt) is formed as exp(L dt / 2)^2 (one exponential per value)
                 if constexpr (MODE == 1) {
                     T e2 = lin_at(a, kxv, iy, dt / 2);
-                    T f = dt / 6 * lin_at(a, kxv, iy, dt);
+                    T f = dt / 6 * (e2 * e2);
                     w = mk(w.x + f * n.x, w.y + f * n.y);
                     av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), e2);
                 } else if constexpr (MODE == 2) {
@@ -424,9 +455,10 @@ struct ColPass {
                     w = mk(w.x + f * n.x, w.y + f * n.y);
                     av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), e2);
                 } else if constexpr (MODE == 3) {
-                    T f = dt / 3 * lin_at(a, kxv, iy, dt / 2);
+                    T e2 = lin_at(a, kxv, iy, dt / 2);
+                    T f = dt / 3 * e2;
                     w = mk(w.x + f * n.x, w.y + f * n.y);
-                    av[r] = scale(mk(o.x + dt * n.x, o.y + dt * n.y), lin_at(a, kxv, iy, dt));
+                    av[r] = scale(mk(o.x + dt * n.x, o.y + dt * n.y), e2 * e2);
                 } else {
                     w = mk(w.x + dt / 6 * n.x, w.y + dt / 6 * n.y);
                     av[r] = w;   // next step: w_old = w_appr = w_new
@@ -466,8 +498,8 @@ struct ColPass {
                 } else {
                     const T kyv = a.kyt[iy];
                     const T k2 = kyv * kyv + kxv * kxv;
-                    const T kk = f == 1 ? kyv : -kxv;
-                    v[r] = (col && (kx != 0 || iy != 0)) ? mk(-w.y * kk / k2, w.x * kk / k2) : mk<T>(0, 0);
+                    const T q = (f == 1 ? kyv : -kxv) / k2;
+                    v[r] = (col && (kx != 0 || iy != 0)) ? mk(-w.y * q, w.x * q) : mk<T>(0, 0);
                     if (owner && kx == 0 && iy == 0) v[r] = mk(f == 1 ? m0 : m1, (T)0);
                 }
             }

@@ -43,6 +43,9 @@ struct Runner {
         HostTables<T> t;
         StepArgs<T> a{};
         host_setup<T>(p, t, a, 1 << 16);
+        // same choice as the C ABI's set_state: pruned transforms under the 1/2
+        // rule when the state is zero outside its ellipse
+        set_pruning<T>(a, p.dealias == AM_DEALIAS_HALF && state_inside_half_mask<T>(w_hat, p.nx, p.ny));
         const int W = Tile<T>::W, nx = p.nx, ny = p.ny;
         const size_t fsz = (size_t)t.nt * W * ny;
         std::vector<cpx<T>> u0(fsz), acc(fsz), fa(fsz), fx(fsz), fy(fsz), P(fsz), Q(fsz);
@@ -64,7 +67,7 @@ struct Runner {
         auto col = [&](int mode) {
             auto go = [&](auto tag) {
                 using CP = ColPass<T, LY, decltype(tag)::value>;
-                launch((t.nt + CP::TILES - 1) / CP::TILES, CP::THREADS, CP::smem_bytes(),
+                launch((a.ntp + CP::TILES - 1) / CP::TILES, CP::THREADS, CP::smem_bytes(),
                        [&](int tid, int bid, unsigned char *sm, auto &sync) { CP::body(a, tid, bid, sm, sync); });
             };
             switch (mode) {

@@ -210,3 +210,39 @@ def test_gpu_step_async_matches_step(am):
     assert np.array_equal(wa, wb) and np.array_equal(ma, mb)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_gpu_half_rule_state_outside_ellipse(am, orc, prec):
+    """A state with modes outside the 1/2-rule ellipse runs the full transforms
+    (the pruned path needs zeros there) and still matches the oracle; the modes
+    outside decay by the integrating factor alone."""
+    nx, ny = 128, 64
+    w0 = np.fft.rfft2(np.random.default_rng(8).standard_normal((ny, nx)))
+    w0[0, 0] = 0
+    sim = am.Solver(nx, ny, 40.0, 20.0, 0.004, 7.0, -0.8, 0.01, dealias="half", precision=prec)
+    sim.set_state(w0, (20.0, -5.0))
+    e = sim.step(4)
+    w, m = sim.get_state()
+    sim.close()
+    p = orc.make_params(nx, ny, 40.0, 20.0, 0.004, 7.0, -0.8, 0.01, dealias="half")
+    wo, mo, eo = orc.run(p, w0, (20.0, -5.0), 4, "f64")
+    tol = 1e-10 if prec == "fp64" else 2e-5
+    assert rel(w, wo) < tol
+    assert np.abs(e - eo).max() <= tol * np.abs(eo).max()
+
+
+def test_gpu_pruned_state_stays_inside_ellipse(am):
+    """Pruned transforms: a band-limited state under the 1/2 rule keeps exact
+    zeros outside the ellipse after many steps."""
+    nx = ny = 256
+    w0 = am.ic_bandlimited(nx, ny, seed=4, kmax=30.0, rms=0.5)
+    sim = am.Solver(nx, ny, 2 * math.pi, 2 * math.pi, 2e-4, 3.5, -0.8, 0.01, gamma0=-0.045, gamma2=2.5e-5,
+                    dealias="half")
+    sim.set_state(w0)
+    sim.step(50)
+    w, _ = sim.get_state()
+    sim.close()
+    mask = np.array([[am.mask_value(nx, ny, "half", ix, iy) for ix in range(nx // 2 + 1)] for iy in range(ny)])
+    assert np.abs(w[mask == 0]).max() == 0.0
+    assert np.abs(w[mask == 1]).max() > 0.0

@@ -82,3 +82,23 @@ def test_emulated_forward_transform(am, emu, n, prec):
     emu.emu_forward(ctypes.byref(p), x.ctypes.data, w.ctypes.data, 0)
     ref = np.fft.rfft2(x.astype(np.float64))
     assert np.abs(w - ref).max() <= (1e-14 if prec else 5e-7) * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("n", [(64, 64), (128, 32), (32, 128)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_emulated_pruned_half_rule(am, orc, emu, n, prec):
+    """1/2 rule with a state inside the ellipse: the kernels skip kx > Nx/4
+    (pruned transforms) and must reproduce the full-transform oracle."""
+    nx, ny = n
+    w0 = am.ic_bandlimited(nx, ny, seed=17, kmax=min(nx, ny) / 8.0, rms=2.0)
+    kw = dict(gamma0=-0.045, gamma2=2.5e-5)
+    p = am.Params(nx, ny, 6.283185307179586, 6.283185307179586, 2e-3, 3.5, -0.8, 0.01, kw["gamma0"],
+                  kw["gamma2"], 1, 1, prec)
+    w, m, e = _emu_run(am, emu, p, w0, (30.0, 10.0), 3)
+    op = orc.make_params(nx, ny, 6.283185307179586, 6.283185307179586, 2e-3, 3.5, -0.8, 0.01, dealias="half", **kw)
+    wo, mo, eo = orc.run(op, w0, (30.0, 10.0), 3, "f64")
+    tol = 1e-13 if prec else 1e-6
+    assert np.linalg.norm(w - wo) / np.linalg.norm(wo) < tol
+    assert np.abs(e - eo).max() <= tol * np.abs(eo).max()
+    mask = orc.mask(nx, ny, "half")
+    assert np.abs(w[mask == 0]).max() == 0.0

@@ -76,6 +76,7 @@ def _load():
         "am_step_profiled": ([hp, ctypes.c_int, dp, dp], ctypes.c_int),
         "am_launches_per_step": ([hp], ctypes.c_int),
         "am_device_bytes": ([hp], ctypes.c_longlong),
+        "am_kx_carried": ([hp], ctypes.c_int),
         "am_status_string": ([ctypes.c_int], ctypes.c_char_p),
         "am_last_error": ([hp], ctypes.c_char_p),
         "am_mask_value": ([ctypes.c_int] * 5, ctypes.c_int),
@@ -100,7 +101,8 @@ lib = _load()
 # Every symbol include/actflow.h declares (checked by the CPU test suite).
 EXPORTED = [
     "am_create", "am_destroy", "am_set_stream", "am_set_state", "am_set_state_real", "am_get_state",
-    "am_step", "am_step_async", "am_sync", "am_step_profiled", "am_launches_per_step", "am_device_bytes", "am_status_string",
+    "am_step", "am_step_async", "am_sync", "am_step_profiled", "am_launches_per_step", "am_device_bytes", "am_kx_carried",
+    "am_status_string",
     "am_last_error", "am_mask_value", "am_ic_bandlimited", "am_spec_read", "am_write_snapshot",
     "am_read_snapshot", "am_append_energy", "am_cli_main",
 ]
@@ -195,6 +197,11 @@ class Solver:
     @property
     def launches_per_step(self):
         return lib.am_launches_per_step(self.h)
+
+    @property
+    def kx_carried(self):
+        """Highest kx the stage fields carry (Nx/4 when the transforms are pruned)."""
+        return lib.am_kx_carried(self.h)
 
     @property
     def device_bytes(self):

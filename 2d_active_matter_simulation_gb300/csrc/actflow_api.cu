@@ -513,6 +513,12 @@ int am_launches_per_step(const am_handle *h) { return h ? 8 : 0; }
 
 long long am_device_bytes(const am_handle *h) { return h ? h->bytes : 0; }
 
+int am_kx_carried(const am_handle *h)
+{
+    if (!h) return -1;
+    return h->fp64 ? h->a64.kxp : h->a32.kxp;
+}
+
 am_status am_ic_bandlimited(int nx, int ny, unsigned long long seed, double kmin, double kmax, double rms,
                             double *w_hat)
 {

@@ -139,11 +139,25 @@ struct DFT {
 template <typename T, int W, int SWZ>
 struct XBuf {
     cpx<T> *d;
+    // additive pads i + (i >> SH): pad(b + r s) = pad(b) + r (s + s >> SH)
+    // whenever s is a multiple of 2^SH, so strided accesses need one index
+    // computation per pass (see at()).
+    static constexpr int SH = SWZ == 0 ? 3 : SWZ == 2 ? 2 : SWZ == 3 ? 4 : 0;
     AF_HDC static constexpr int pad(int i)
     {
         if constexpr (SWZ == 0) return i + (i >> 3);
         else if constexpr (SWZ == 1) return i ^ ((i >> 4) & 15);
-        else return i + (i >> 2);
+        else if constexpr (SWZ == 2) return i + (i >> 2);
+        else return i + (i >> 4);
+    }
+    // Slot of element base + r * STRIDE for transform c.
+    template <int STRIDE>
+    AF_HD int at(int base, int r, int c) const
+    {
+        if constexpr (SWZ != 1 && (STRIDE % (1 << SH)) == 0)
+            return (pad(base) + r * (STRIDE + (STRIDE >> SH))) * W + c;
+        else
+            return pad(base + r * STRIDE) * W + c;
     }
     // slots needed for L elements
     AF_HDC static constexpr int slots(int L)
@@ -215,12 +229,32 @@ struct BlockFFT {
     static constexpr int LOGR1 = LOGL % LOGR;
     static constexpr int R1 = 1 << LOGR1;          // first-pass radix (1: none)
     static constexpr int NPASS = (LOGL - LOGR1) / LOGR;
+    static constexpr int NEXCH = NPASS - 1 + (LOGR1 > 0 ? 1 : 0);   // shared-memory exchanges
 
+    // Exchanges alternate between two buffers b0, b1 (b1 may equal b0): with
+    // two buffers one barrier per exchange suffices, because the barrier that
+    // publishes exchange e also orders every read of exchange e-1 before the
+    // writes of exchange e+1.  One barrier at entry separates this transform
+    // from earlier users of the buffers.
+    template <class Buf, class Sync>
+    static AF_HD void run(cpx<T> (&v)[R], int j, int c, const Buf &b0, const Buf &b1, const cpx<T> *tw, int TWS,
+                          Sync &&sync)
+    {
+        if constexpr (NEXCH > 0) sync();
+        run_passes<0>(v, j, c, b0, b1, tw, TWS, sync);
+    }
     template <class Buf, class Sync>
     static AF_HD void run(cpx<T> (&v)[R], int j, int c, const Buf &buf, const cpx<T> *tw, int TWS, Sync &&sync)
     {
-        int Ns = 1;
-        bool in_regs = true;
+        if constexpr (NEXCH > 0) sync();
+        run_passes<1>(v, j, c, buf, buf, tw, TWS, sync);
+    }
+
+    template <int SINGLE, class Buf, class Sync>
+    static AF_HD void run_passes(cpx<T> (&v)[R], int j, int c, const Buf &b0, const Buf &b1, const cpx<T> *tw,
+                                 int TWS, Sync &&sync)
+    {
+        int e = 0;   // exchange counter: buffer e % 2
         if constexpr (LOGR1 > 0) {
             constexpr int G = R / R1;
 #pragma unroll
@@ -232,44 +266,54 @@ struct BlockFFT {
 #pragma unroll
                 for (int r1 = 0; r1 < R1; r1++) v[q + G * r1] = u[r1];
             }
-            sync();
+            const Buf &b = b0;
 #pragma unroll
             for (int q = 0; q < G; q++) {
-                int b = j + q * TPC;
+                const int base = (j + q * TPC) * R1;
 #pragma unroll
-                for (int r1 = 0; r1 < R1; r1++) buf.put(b * R1 + r1, c, v[q + G * r1]);
+                for (int r1 = 0; r1 < R1; r1++) b.d[b.template at<1>(base, r1, c)] = v[q + G * r1];
             }
             sync();
-            Ns = R1;
-            in_regs = false;
+            e = 1;
         }
+        pass<0, LOGR1 == 0, SINGLE>(v, j, c, b0, b1, tw, TWS, sync, e);
+    }
+
+    // Radix-R pass number P (sub-transform size NS = R1 * R^P).
+    template <int P, bool FROM_REGS, int SINGLE, class Buf, class Sync>
+    static AF_HD void pass(cpx<T> (&v)[R], int j, int c, const Buf &b0, const Buf &b1, const cpx<T> *tw, int TWS,
+                           Sync &&sync, int e)
+    {
+        if constexpr (P < NPASS) {
+            constexpr int NS = R1 * ipow(R, P);
+            if constexpr (!FROM_REGS) {
+                const Buf &b = (SINGLE || (e & 1) == 1) ? b0 : b1;   // buffer written by exchange e-1
 #pragma unroll
-        for (int p = 0; p < NPASS; p++) {
-            if (!in_regs) {
-#pragma unroll
-                for (int r = 0; r < R; r++) v[r] = buf.get(j + r * TPC, c);
+                for (int r = 0; r < R; r++) v[r] = b.d[b.template at<TPC>(j, r, c)];
             }
-            in_regs = false;
-            if (Ns > 1) {
-                int k = j & (Ns - 1);
-                int step = (L / (Ns * R)) * k * TWS;   // twiddle index of W^{k}
+            if constexpr (NS > 1) {
+                const int k = j & (NS - 1);
+                const int step = (L / (NS * R)) * k * TWS;   // twiddle index of W^{k}
                 cpx<T> w[R];
                 twiddles<R>(w, tw, step);
 #pragma unroll
                 for (int r = 1; r < R; r++) v[r] = SIGN < 0 ? cmul(v[r], w[r]) : cmulc(v[r], w[r]);
             }
             DFT<R, SIGN, T>::run(v);
-            if (p < NPASS - 1) {
-                int k = j & (Ns - 1);
-                int base = (j - k) * R + k;
-                sync();
+            if constexpr (P < NPASS - 1) {
+                const Buf &b = (SINGLE || (e & 1) == 0) ? b0 : b1;
+                const int k = j & (NS - 1);
+                const int base = (j - k) * R + k;
+                if (SINGLE && e > 0) sync();   // one buffer: earlier reads must finish
 #pragma unroll
-                for (int r = 0; r < R; r++) buf.put(base + r * Ns, c, v[r]);
+                for (int r = 0; r < R; r++) b.d[b.template at<NS>(base, r, c)] = v[r];
                 sync();
-                Ns *= R;
+                pass<P + 1, false, SINGLE>(v, j, c, b0, b1, tw, TWS, sync, e + 1);
             }
         }
     }
+
+    static constexpr int ipow(int b, int p) { return p == 0 ? 1 : b * ipow(b, p - 1); }
 };
 
 }  // namespace af

@@ -28,7 +28,7 @@ struct RowFwd {
         const bool active = yy < ny;
         const int y = active ? yy : ny - 1;
         const int nx = 2 * M;
-        Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * BUFS};
+        Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * 2 * BUFS};
         cpx<T> v[R];
 #pragma unroll
         for (int r = 0; r < R; r++) {

@@ -148,18 +148,26 @@ struct RowPass {
     static constexpr int ROWS = TPC >= 128 ? 1 : 128 / TPC;
     static constexpr int THREADS = ROWS * TPC;
     static constexpr int MINB = sizeof(T) == 4 ? 4 : 2;   // resident CTAs per SM (register cap)
-    using Buf = XBuf<T, 1, sizeof(T) == 4 ? 1 : 2>;
-    static constexpr int BUFS = (Buf::slots(M) + 7) / 8 * 8;   // complex slots per row
+    using Buf = XBuf<T, 1, sizeof(T) == 4 ? 3 : 2>;
+    static constexpr int BUFS = (Buf::slots(M) + 7) / 8 * 8;   // complex slots per buffer
 
-    static constexpr size_t smem_bytes() { return (size_t)ROWS * BUFS * sizeof(cpx<T>); }
+    // two exchange buffers per row (double buffering)
+    static constexpr size_t smem_bytes() { return (size_t)ROWS * 2 * BUFS * sizeof(cpx<T>); }
 
     // C2R pre-processing of X(k), X(M-k): Z(k) = E + i O with
     // E = X(k) + conj X(M-k), O = (X(k) - conj X(M-k)) exp(2 pi i k / Nx).
+    // A row's element kx lives at row_base + (kx / W) * Ny * W + kx % W.  For
+    // k = j + r TPC with TPC a multiple of W this is a per-thread base plus
+    // r * TPC * Ny: one index computation per transform.
     static AF_HD cpx<T> pack(const cpx<T> *src, int k, int y, int ny, int kxp, const cpx<T> *twx)
     {
         // entries above kxp are zero by construction (pruned transforms) and are not read
         cpx<T> A = k <= kxp ? src[tidx<T>(k, y, ny)] : mk<T>(0, 0);
         cpx<T> B = M - k <= kxp ? src[tidx<T>(M - k, y, ny)] : mk<T>(0, 0);
+        return pack_vals(A, B, k, twx);
+    }
+    static AF_HD cpx<T> pack_vals(cpx<T> A, cpx<T> B, int k, const cpx<T> *twx)
+    {
         if (k == 0) {   // X(0), X(M): imaginary parts dropped, as a half-plane C2R does
             A.y = 0;
             B.y = 0;
@@ -168,6 +176,80 @@ struct RowPass {
         cpx<T> E = A + B;
         cpx<T> O = cmulc(A - B, ldtw(twx, k));
         return mk(E.x - O.y, E.y + O.x);
+    }
+
+    static AF_HD void load_pack(cpx<T> (&v)[R], const cpx<T> *src, int j, int y, int ny, int kxp,
+                                const cpx<T> *twx)
+    {
+        constexpr int W = Tile<T>::W;
+        if constexpr (TPC % W == 0) {
+            // k = j + r TPC and M - k = (M - j) - r TPC share one base index each
+            const cpx<T> *pa = src + tidx<T>(j, y, ny);
+            const cpx<T> *pb = src + tidx<T>(M - j, y, ny);
+            const size_t stride = (size_t)(TPC / W) * ny * W;
+            cpx<T> A[R], B[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int k = j + r * TPC;
+                A[r] = k <= kxp ? pa[r * stride] : mk<T>(0, 0);
+                B[r] = M - k <= kxp ? pb[-(long long)(r * stride)] : mk<T>(0, 0);
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++) v[r] = pack_vals(A[r], B[r], j + r * TPC, twx);
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; r++) v[r] = pack(src, j + r * TPC, y, ny, kxp, twx);
+        }
+    }
+
+    // Sum (t0, t1, t2) over the TPC threads of a row; the result is valid in
+    // thread j = 0.  GPU: warp shuffles, then one shared-memory step across the
+    // row's warps.  Elsewhere: a shared-memory tree.
+    template <class Sync>
+    static AF_HD void row_sum3(double &t0, double &t1, double &t2, int j, double *scratch, Sync &&sync)
+    {
+#ifdef __CUDA_ARCH__
+        if constexpr (TPC >= 32) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+                t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+                t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+            }
+            constexpr int NW = TPC / 32;
+            sync();
+            if ((j & 31) == 0) {
+                scratch[(j >> 5) * 3 + 0] = t0;
+                scratch[(j >> 5) * 3 + 1] = t1;
+                scratch[(j >> 5) * 3 + 2] = t2;
+            }
+            sync();
+            if (j == 0) {
+                for (int w = 1; w < NW; w++) {
+                    t0 += scratch[w * 3 + 0];
+                    t1 += scratch[w * 3 + 1];
+                    t2 += scratch[w * 3 + 2];
+                }
+            }
+            return;
+        }
+#endif
+        sync();
+        scratch[j] = t0;
+        scratch[TPC + j] = t1;
+        scratch[2 * TPC + j] = t2;
+        sync();
+        for (int s = TPC / 2; s > 0; s >>= 1) {
+            if (j < s) {
+                scratch[j] += scratch[j + s];
+                scratch[TPC + j] += scratch[TPC + j + s];
+                scratch[2 * TPC + j] += scratch[2 * TPC + j + s];
+            }
+            sync();
+        }
+        t0 = scratch[0];
+        t1 = scratch[TPC];
+        t2 = scratch[2 * TPC];
     }
 
     // R2C post-processing: X(k) = E + exp(-2 pi i k / Nx) O with
@@ -188,23 +270,21 @@ struct RowPass {
         const bool active = yy < a.ny;
         const int y = active ? yy : a.ny - 1;   // inactive rows recompute the last row, never store
         const int ny = a.ny;
-        Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * BUFS};
+        Buf b0{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * 2 * BUFS};
+        Buf b1{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * 2 * BUFS + BUFS};
 
         // ---- C2R along x of uy, ux (kept) and w (consumed by the products)
         cpx<T> zy[R], zx[R], v[R];
-#pragma unroll
-        for (int r = 0; r < R; r++) v[r] = pack(a.fy, j + r * TPC, y, ny, a.kxp, a.twx);
-        FFTi::run(v, j, 0, buf, a.twx, 2, sync);
+        load_pack(v, a.fy, j, y, ny, a.kxp, a.twx);
+        FFTi::run(v, j, 0, b0, b1, a.twx, 2, sync);
 #pragma unroll
         for (int r = 0; r < R; r++) zy[r] = v[r];
-#pragma unroll
-        for (int r = 0; r < R; r++) v[r] = pack(a.fx, j + r * TPC, y, ny, a.kxp, a.twx);
-        FFTi::run(v, j, 0, buf, a.twx, 2, sync);
+        load_pack(v, a.fx, j, y, ny, a.kxp, a.twx);
+        FFTi::run(v, j, 0, b0, b1, a.twx, 2, sync);
 #pragma unroll
         for (int r = 0; r < R; r++) zx[r] = v[r];
-#pragma unroll
-        for (int r = 0; r < R; r++) v[r] = pack(a.fa, j + r * TPC, y, ny, a.kxp, a.twx);
-        FFTi::run(v, j, 0, buf, a.twx, 2, sync);
+        load_pack(v, a.fa, j, y, ny, a.kxp, a.twx);
+        FFTi::run(v, j, 0, b0, b1, a.twx, 2, sync);
 
         // ---- real-space products; z[r] holds x = 2n (real part) and 2n + 1
         // (imaginary part), n = j + r * TPC.  P overwrites zx, Q overwrites zy.
@@ -222,46 +302,35 @@ struct RowPass {
             zy[r] = mk(lam * w0 * uy0 - bet * s0 * ux0, lam * w1 * uy1 - bet * s1 * ux1);
         }
 
-        // ---- row sums (double tree over the row's TPC threads; the exchange
-        // buffer doubles as scratch)
+        // ---- row sums of |u|^2, |u|^2 ux, |u|^2 uy in double over the row
         {
-            double *red = reinterpret_cast<double *>(buf.d);
-            sync();
-            red[j] = (double)se;
-            red[TPC + j] = (double)sx;
-            red[2 * TPC + j] = (double)sy;
-            sync();
-            for (int s = TPC / 2; s > 0; s >>= 1) {
-                if (j < s) {
-                    red[j] += red[j + s];
-                    red[TPC + j] += red[TPC + j + s];
-                    red[2 * TPC + j] += red[2 * TPC + j + s];
-                }
-                sync();
-            }
+            double t0 = se, t1 = sx, t2 = sy;
+            row_sum3(t0, t1, t2, j, reinterpret_cast<double *>(b0.d), sync);
             if (active && j == 0) {
-                a.rowp[(size_t)y * 3 + 0] = red[0];
-                a.rowp[(size_t)y * 3 + 1] = red[TPC];
-                a.rowp[(size_t)y * 3 + 2] = red[2 * TPC];
+                a.rowp[(size_t)y * 3 + 0] = t0;
+                a.rowp[(size_t)y * 3 + 1] = t1;
+                a.rowp[(size_t)y * 3 + 2] = t2;
             }
         }
 
         // ---- R2C along x of P and Q
+        // The pairing exchange uses the buffer the transform's last pass did not read.
+        const Buf &pb = (FFTf::NEXCH & 1) ? b1 : b0;
 #pragma unroll
         for (int f = 0; f < 2; f++) {
 #pragma unroll
             for (int r = 0; r < R; r++) v[r] = f == 0 ? zx[r] : zy[r];
-            FFTf::run(v, j, 0, buf, a.twx, 2, sync);
-            sync();
+            FFTf::run(v, j, 0, b0, b1, a.twx, 2, sync);
+            if constexpr (FFTf::NEXCH == 0) sync();
 #pragma unroll
-            for (int r = 0; r < R; r++) buf.put(j + r * TPC, 0, v[r]);
+            for (int r = 0; r < R; r++) pb.put(j + r * TPC, 0, v[r]);
             sync();
             cpx<T> *dst = f == 0 ? a.P : a.Q;
             const int kend = a.ntp * Tile<T>::W;   // the column pass reads kx < kend
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 int k = j + r * TPC;
-                if (active && k < kend) dst[tidx<T>(k, y, ny)] = unpack(v[r], buf.get((M - k) & (M - 1), 0), ldtw(a.twx, k));
+                if (active && k < kend) dst[tidx<T>(k, y, ny)] = unpack(v[r], pb.get((M - k) & (M - 1), 0), ldtw(a.twx, k));
             }
             if (active && j == 0 && M < kend) {   // kx = M: E(0) - O(0)
                 dst[tidx<T>(M, y, ny)] = unpack(v[0], v[0], mk<T>(-1, 0));

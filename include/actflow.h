@@ -120,6 +120,11 @@ am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double co
 /* Number of kernel launches one step makes (for accounting). */
 int am_launches_per_step(const am_handle *h);
 
+/* Highest kx index the stage fields carry: Nx/2 for the full transforms,
+ * Nx/4 when the 1/2 rule lets the solver prune the transforms (the state
+ * loaded last is zero outside the rule's ellipse).  -1 for a NULL handle. */
+int am_kx_carried(const am_handle *h);
+
 /* Device bytes held by the handle. */
 long long am_device_bytes(const am_handle *h);
 

@@ -20,7 +20,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/actflow.h"
+#include "actflow.h"
 #include "host_tables.h"
 #include "kernels.h"
 

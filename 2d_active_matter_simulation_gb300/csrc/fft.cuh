@@ -19,6 +19,8 @@
 //  * Transforms are unnormalised; SIGN = -1 forward, +1 inverse.
 #pragma once
 
+#include <type_traits>
+
 #ifdef __CUDACC__
 #define AF_HD __host__ __device__ __forceinline__
 #define AF_HDC __host__ __device__
@@ -61,33 +63,50 @@ AF_HD cpx<T> conj(cpx<T> a) { return mk(a.x, -a.y); }
 template <typename T>
 AF_HD cpx<T> scale(cpx<T> a, T s) { return mk(a.x * s, a.y * s); }
 
-// Multiply by exp(SIGN * 2 pi i Q / R) for compile-time Q, R (R <= 16).
+// Multiply by exp(SIGN * 2 pi i Q / R) for compile-time Q, R (R <= 32).
 // Multiples of pi/2 are exact sign swaps; the remaining angles are multiples
-// of pi/8, whose cosines and sines are the constants below.
+// of pi/16, whose cosines are the constants below.
 template <int Q, int R, int SIGN, typename T>
 AF_HD cpx<T> rot(cpx<T> a)
 {
-    constexpr int N16 = (16 / R) * Q;          // angle in units of 2 pi / 16
-    constexpr int q = ((N16 % 16) + 16) % 16;
+    constexpr int N32 = (32 / R) * Q;          // angle in units of 2 pi / 32
+    constexpr int q = ((N32 % 32) + 32) % 32;
     if constexpr (q == 0) {
         return a;
-    } else if constexpr (q == 4) {             // pi/2: multiply by SIGN * i
+    } else if constexpr (q == 8) {             // pi/2: multiply by SIGN * i
         return SIGN > 0 ? mk(-a.y, a.x) : mk(a.y, -a.x);
-    } else if constexpr (q == 8) {
+    } else if constexpr (q == 16) {
         return mk(-a.x, -a.y);
-    } else if constexpr (q == 12) {
+    } else if constexpr (q == 24) {
         return SIGN > 0 ? mk(a.y, -a.x) : mk(-a.y, a.x);
     } else {
-        // cos and sin of 2 pi k / 16 for k = 0..3 (first quadrant)
-        constexpr double C[4] = {1.0, 0.92387953251128675613, 0.70710678118654752440, 0.38268343236508977173};
-        constexpr int qq = q % 4;               // offset inside the quadrant
-        constexpr int quad = q / 4;
-        // cos(q*2pi/16), sin(q*2pi/16) from quadrant symmetry
-        constexpr double c0 = C[qq], s0 = C[4 - qq == 4 ? 0 : 4 - qq];
+        // cos(2 pi k / 32), k = 0..8
+        constexpr double C[9] = {1.0,
+                                 0.98078528040323044913,
+                                 0.92387953251128675613,
+                                 0.83146961230254523708,
+                                 0.70710678118654752440,
+                                 0.55557023301960222474,
+                                 0.38268343236508977173,
+                                 0.19509032201612826785,
+                                 0.0};
+        constexpr int qq = q % 8;              // offset inside the quadrant
+        constexpr int quad = q / 8;
+        constexpr double c0 = C[qq], s0 = C[8 - qq];
         constexpr double cs = quad == 0 ? c0 : quad == 1 ? -s0 : quad == 2 ? -c0 : s0;
         constexpr double sn = quad == 0 ? s0 : quad == 1 ? c0 : quad == 2 ? -s0 : -c0;
         const T c = (T)cs, s = (T)(SIGN * sn);
         return mk(a.x * c - a.y * s, a.x * s + a.y * c);
+    }
+}
+
+// Calls f(std::integral_constant<int, I>) for I = I0 .. N-1 (compile-time loop).
+template <int I0, int N, class Fn>
+AF_HD void static_for(Fn &&f)
+{
+    if constexpr (I0 < N) {
+        f(std::integral_constant<int, I0>{});
+        static_for<I0 + 1, N>(f);
     }
 }
 
@@ -142,13 +161,14 @@ struct XBuf {
     // additive pads i + (i >> SH): pad(b + r s) = pad(b) + r (s + s >> SH)
     // whenever s is a multiple of 2^SH, so strided accesses need one index
     // computation per pass (see at()).
-    static constexpr int SH = SWZ == 0 ? 3 : SWZ == 2 ? 2 : SWZ == 3 ? 4 : 0;
+    static constexpr int SH = SWZ == 0 ? 3 : SWZ == 2 ? 2 : SWZ == 3 ? 4 : SWZ == 4 ? 5 : 0;
     AF_HDC static constexpr int pad(int i)
     {
         if constexpr (SWZ == 0) return i + (i >> 3);
         else if constexpr (SWZ == 1) return i ^ ((i >> 4) & 15);
         else if constexpr (SWZ == 2) return i + (i >> 2);
-        else return i + (i >> 4);
+        else if constexpr (SWZ == 3) return i + (i >> 4);
+        else return i + (i >> 5);
     }
     // Slot of element base + r * STRIDE for transform c.
     template <int STRIDE>
@@ -199,7 +219,32 @@ AF_HD cpx<double> ldtw(const cpx<double> *tw, int idx)
 template <int R, typename T>
 AF_HD void twiddles(cpx<T> *w, const cpx<T> *tw, int step)
 {
-    if constexpr (sizeof(T) == 8 || R <= 2) {
+    if constexpr (sizeof(T) == 4 && R <= 8 && R > 2) {
+        // radix <= 8, FP32: one table load; W^2k, W^4k by squaring and the
+        // rest by products (at most three roundings deep, a few ulp).
+        w[1] = ldtw(tw, step);
+        w[2] = cmul(w[1], w[1]);
+        w[3] = cmul(w[2], w[1]);
+        if constexpr (R == 8) {
+            w[4] = cmul(w[2], w[2]);
+            w[5] = cmul(w[4], w[1]);
+            w[6] = cmul(w[4], w[2]);
+            w[7] = cmul(w[4], w[3]);
+        }
+    } else if constexpr (sizeof(T) == 4 && R == 16) {
+        // radix 16, FP32: W^k and W^4k loaded, the rest by products (at most
+        // four roundings deep)
+        w[1] = ldtw(tw, step);
+        w[4] = ldtw(tw, 4 * step);
+        w[2] = cmul(w[1], w[1]);
+        w[3] = cmul(w[2], w[1]);
+        w[5] = cmul(w[4], w[1]);
+        w[6] = cmul(w[4], w[2]);
+        w[7] = cmul(w[4], w[3]);
+        w[8] = cmul(w[4], w[4]);
+#pragma unroll
+        for (int r = 9; r < 16; r++) w[r] = cmul(w[8], w[r - 8]);
+    } else if constexpr (sizeof(T) == 8 || R <= 2) {
 #pragma unroll
         for (int r = 1; r < R; r++) w[r] = ldtw(tw, r * step);
     } else {
@@ -216,6 +261,11 @@ AF_HD void twiddles(cpx<T> *w, const cpx<T> *tw, int step)
             w[8] = ldtw(tw, 8 * step);
 #pragma unroll
             for (int r = 9; r < 16; r++) w[r] = cmul(w[8], w[r - 8]);
+        }
+        if constexpr (R >= 32) {
+            w[16] = ldtw(tw, 16 * step);
+#pragma unroll
+            for (int r = 17; r < 32; r++) w[r] = cmul(w[16], w[r - 16]);
         }
     }
 }
@@ -294,10 +344,20 @@ struct BlockFFT {
             if constexpr (NS > 1) {
                 const int k = j & (NS - 1);
                 const int step = (L / (NS * R)) * k * TWS;   // twiddle index of W^{k}
-                cpx<T> w[R];
-                twiddles<R>(w, tw, step);
+                if constexpr (R >= 32) {
+                    // radix 32: each twiddle is read from the (L1-resident) table
+                    // right before use, so no twiddle array is held in registers
 #pragma unroll
-                for (int r = 1; r < R; r++) v[r] = SIGN < 0 ? cmul(v[r], w[r]) : cmulc(v[r], w[r]);
+                    for (int r = 1; r < R; r++) {
+                        const cpx<T> w = ldtw(tw, r * step);
+                        v[r] = SIGN < 0 ? cmul(v[r], w) : cmulc(v[r], w);
+                    }
+                } else {
+                    cpx<T> w[R];
+                    twiddles<R>(w, tw, step);
+#pragma unroll
+                    for (int r = 1; r < R; r++) v[r] = SIGN < 0 ? cmul(v[r], w[r]) : cmulc(v[r], w[r]);
+                }
             }
             DFT<R, SIGN, T>::run(v);
             if constexpr (P < NPASS - 1) {

@@ -7,10 +7,10 @@
 namespace af {
 
 template <typename T, int LOG>
-__global__ void __launch_bounds__(RowPass<T, LOG>::THREADS, RowPass<T, LOG>::MINB) k_row(StepArgs<T> a)
+__global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::MINB) k_row(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    RowPass<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+    RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
 template <typename T, int LOG, int MODE>
@@ -69,7 +69,7 @@ struct Fill {
     static void run(KernelTable<T> &t)
     {
         t.row[LOG] = k_row<T, LOG>;
-        t.row_shape[LOG] = {RowPass<T, LOG>::THREADS, RowPass<T, LOG>::smem_bytes(), RowPass<T, LOG>::ROWS};
+        t.row_shape[LOG] = {RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::smem_bytes(), RowKernel<T, LOG>::ROWS};
         t.col[LOG][0] = k_col<T, LOG, 0>;
         t.col[LOG][1] = k_col<T, LOG, 1>;
         t.col[LOG][2] = k_col<T, LOG, 2>;

@@ -125,6 +125,9 @@ struct ColMask {
     }
 };
 
+// Stops the compiler from moving memory accesses across this point.
+AF_HD void compiler_fence() { asm volatile("" ::: "memory"); }
+
 AF_HD float expT(float x) { return expf(x); }
 AF_HD double expT(double x) { return exp(x); }
 
@@ -147,8 +150,10 @@ struct RowPass {
     static constexpr int TPC = FFTi::TPC;
     static constexpr int ROWS = TPC >= 128 ? 1 : 128 / TPC;
     static constexpr int THREADS = ROWS * TPC;
-    static constexpr int MINB = sizeof(T) == 4 ? 4 : 2;   // resident CTAs per SM (register cap)
-    using Buf = XBuf<T, 1, sizeof(T) == 4 ? 3 : 2>;
+    // resident CTAs per SM requested from the compiler: caps registers at 128 (FP32) / 255 (FP64)
+    static constexpr int MINB = sizeof(T) == 4 ? (THREADS >= 256 ? 2 : 4) : 1;
+    static constexpr bool WARP_SYNC = false;
+    using Buf = XBuf<T, 1, sizeof(T) == 4 ? 1 : 2>;
     static constexpr int BUFS = (Buf::slots(M) + 7) / 8 * 8;   // complex slots per buffer
 
     // two exchange buffers per row (double buffering)
@@ -178,6 +183,56 @@ struct RowPass {
         return mk(E.x - O.y, E.y + O.x);
     }
 
+    // X(k) and X(M - k) for k = j + r TPC (zero above kxp, not read).
+    static AF_HD void load_pairs(cpx<T> (&A)[R], cpx<T> (&B)[R], const cpx<T> *src, int j, int y, int ny, int kxp)
+    {
+        constexpr int W = Tile<T>::W;
+        if constexpr (TPC % W == 0) {
+            const cpx<T> *pa = src + tidx<T>(j, y, ny);
+            const cpx<T> *pb = src + tidx<T>(M - j, y, ny);
+            const size_t stride = (size_t)(TPC / W) * ny * W;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int k = j + r * TPC;
+                A[r] = k <= kxp ? pa[r * stride] : mk<T>(0, 0);
+                B[r] = M - k <= kxp ? pb[-(long long)(r * stride)] : mk<T>(0, 0);
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int k = j + r * TPC;
+                A[r] = k <= kxp ? src[tidx<T>(k, y, ny)] : mk<T>(0, 0);
+                B[r] = M - k <= kxp ? src[tidx<T>(M - k, y, ny)] : mk<T>(0, 0);
+            }
+        }
+    }
+    // The pre/post-processing twiddle W^k = exp(-2 pi i k / Nx) for
+    // k = j + r TPC equals W^j * exp(-2 pi i r / (2R)) (Nx = 2 R TPC): one table
+    // value per thread (wj) times a compile-time rotation.
+    static AF_HD void pack_pairs(cpx<T> (&v)[R], const cpx<T> (&A)[R], const cpx<T> (&B)[R], cpx<T> wj, int j)
+    {
+        static_for<0, R>([&](auto rc) {
+            constexpr int r = decltype(rc)::value;
+            cpx<T> a = A[r], b = conj(B[r]);
+            if (r == 0 && j == 0) {   // X(0), X(M): imaginary parts dropped, as a half-plane C2R does
+                a.y = 0;
+                b.y = 0;
+            }
+            const cpx<T> E = a + b;
+            const cpx<T> O = rot<r, 2 * R, +1>(cmulc(a - b, wj));   // (A - conj B) conj(W^k)
+            v[r] = mk(E.x - O.y, E.y + O.x);
+        });
+    }
+    // X(k) = E + W^k O for k = j + r TPC (see unpack); Bp = Z(M - k).
+    template <int r>
+    static AF_HD cpx<T> unpack_r(cpx<T> A, cpx<T> Bp, cpx<T> wj)
+    {
+        const cpx<T> B = conj(Bp);
+        const cpx<T> E = scale(A + B, (T)0.5);
+        const cpx<T> D = scale(A - B, (T)0.5);
+        return E + rot<r, 2 * R, -1>(cmul(mk(D.y, -D.x), wj));
+    }
+
     static AF_HD void load_pack(cpx<T> (&v)[R], const cpx<T> *src, int j, int y, int ny, int kxp,
                                 const cpx<T> *twx)
     {
@@ -187,15 +242,13 @@ struct RowPass {
             const cpx<T> *pa = src + tidx<T>(j, y, ny);
             const cpx<T> *pb = src + tidx<T>(M - j, y, ny);
             const size_t stride = (size_t)(TPC / W) * ny * W;
-            cpx<T> A[R], B[R];
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 const int k = j + r * TPC;
-                A[r] = k <= kxp ? pa[r * stride] : mk<T>(0, 0);
-                B[r] = M - k <= kxp ? pb[-(long long)(r * stride)] : mk<T>(0, 0);
+                cpx<T> A = k <= kxp ? pa[r * stride] : mk<T>(0, 0);
+                cpx<T> B = M - k <= kxp ? pb[-(long long)(r * stride)] : mk<T>(0, 0);
+                v[r] = pack_vals(A, B, k, twx);
             }
-#pragma unroll
-            for (int r = 0; r < R; r++) v[r] = pack_vals(A[r], B[r], j + r * TPC, twx);
         } else {
 #pragma unroll
             for (int r = 0; r < R; r++) v[r] = pack(src, j + r * TPC, y, ny, kxp, twx);
@@ -273,17 +326,32 @@ struct RowPass {
         Buf b0{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * 2 * BUFS};
         Buf b1{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * 2 * BUFS + BUFS};
 
-        // ---- C2R along x of uy, ux (kept) and w (consumed by the products)
+        // ---- C2R along x of uy, ux (kept) and w (consumed by the products).
+        // The Hermitian pairs of the next field are loaded before the current
+        // field's transform, so their latency overlaps the FFT.
+        const cpx<T> wj = ldtw(a.twx, j);
         cpx<T> zy[R], zx[R], v[R];
-        load_pack(v, a.fy, j, y, ny, a.kxp, a.twx);
+        {
+            cpx<T> A[R], B[R];
+            load_pairs(A, B, a.fy, j, y, ny, a.kxp);
+            pack_pairs(v, A, B, wj, j);
+        }
         FFTi::run(v, j, 0, b0, b1, a.twx, 2, sync);
 #pragma unroll
         for (int r = 0; r < R; r++) zy[r] = v[r];
-        load_pack(v, a.fx, j, y, ny, a.kxp, a.twx);
+        {
+            cpx<T> A[R], B[R];
+            load_pairs(A, B, a.fx, j, y, ny, a.kxp);
+            pack_pairs(v, A, B, wj, j);
+        }
         FFTi::run(v, j, 0, b0, b1, a.twx, 2, sync);
 #pragma unroll
         for (int r = 0; r < R; r++) zx[r] = v[r];
-        load_pack(v, a.fa, j, y, ny, a.kxp, a.twx);
+        {
+            cpx<T> A[R], B[R];
+            load_pairs(A, B, a.fa, j, y, ny, a.kxp);
+            pack_pairs(v, A, B, wj, j);
+        }
         FFTi::run(v, j, 0, b0, b1, a.twx, 2, sync);
 
         // ---- real-space products; z[r] holds x = 2n (real part) and 2n + 1
@@ -327,11 +395,11 @@ struct RowPass {
             sync();
             cpx<T> *dst = f == 0 ? a.P : a.Q;
             const int kend = a.ntp * Tile<T>::W;   // the column pass reads kx < kend
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-                int k = j + r * TPC;
-                if (active && k < kend) dst[tidx<T>(k, y, ny)] = unpack(v[r], pb.get((M - k) & (M - 1), 0), ldtw(a.twx, k));
-            }
+            static_for<0, R>([&](auto rc) {
+                constexpr int r = decltype(rc)::value;
+                const int k = j + r * TPC;
+                if (active && k < kend) dst[tidx<T>(k, y, ny)] = unpack_r<r>(v[r], pb.get((M - k) & (M - 1), 0), wj);
+            });
             if (active && j == 0 && M < kend) {   // kx = M: E(0) - O(0)
                 dst[tidx<T>(M, y, ny)] = unpack(v[0], v[0], mk<T>(-1, 0));
             }
@@ -339,6 +407,9 @@ struct RowPass {
         }
     }
 };
+
+template <typename T, int LOGNX>
+using RowKernel = RowPass<T, LOGNX>;
 
 // --------------------------------------------------------------- column pass
 // One tile of W adjacent kx columns per group of W * TPC threads (lane c =

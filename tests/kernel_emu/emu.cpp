@@ -63,7 +63,7 @@ struct Runner {
         sc.m_new[0] = mean[0];
         sc.m_new[1] = mean[1];
         sc.nan_step = -1;
-        using RP = RowPass<T, LX>;
+        using RP = RowKernel<T, LX>;
         auto col = [&](int mode) {
             auto go = [&](auto tag) {
                 using CP = ColPass<T, LY, decltype(tag)::value>;

@@ -35,7 +35,31 @@ NX = NY = 2048
 PARAMS = dict(lx=2 * math.pi, ly=2 * math.pi, dt=1e-4, lam=3.5, alpha=-0.8, beta=0.01,
               gamma0=-0.045, gamma2=2.5e-5, dealias="half")
 SEED = 7
+PRECISION = "fp32"
 WORKLOAD = "IF-RK4 vorticity step, 2048^2, FP32, dt=1e-4, 1/2-rule dealiasing, band-limited seed 7"
+# --config 0: the 256^2 plain-method run (dt 5e-4, the reference's own mask,
+# which keeps every mode at 256^2), seed 42; --precision selects FP32 / FP64.
+PRESETS = {
+    0: dict(n=256, dt=5e-4, dealias="reference", seed=42),
+    1: dict(n=2048, dt=1e-4, dealias="half", seed=7),
+}
+
+
+def apply_preset(cfg, precision):
+    global NX, NY, SEED, PRECISION, WORKLOAD
+    p = PRESETS[cfg]
+    NX = NY = p["n"]
+    SEED = p["seed"]
+    PARAMS["dt"] = p["dt"]
+    PARAMS["dealias"] = p["dealias"]
+    PRECISION = precision
+    WORKLOAD = (f"IF-RK4 vorticity step, {NX}^2, {precision.upper()}, dt={p['dt']:g}, "
+                f"{'1/2-rule' if p['dealias'] == 'half' else 'reference-mask'} dealiasing, band-limited seed {SEED}")
+
+
+# DRAM read + write bytes per launch of each pass for this workload, from the
+# ncu capture summarised in profiles/k_row_k_col_2048_fp32_full.md
+NCU_TRAFFIC = {"row": 25.430e6 + 0.341e6, "col": 25.508e6 + 0.572e6}
 
 
 def peaks():
@@ -106,11 +130,11 @@ def oracle_steps(nsteps, threads=0):
     import oracle
     import importlib
     am = importlib.import_module("2d_active_matter_simulation_gb300")
-    w0 = am.ic_bandlimited(NX, NY, SEED).astype(np.complex64)
+    w0 = am.ic_bandlimited(NX, NY, SEED).astype(np.complex64 if PRECISION == "fp32" else np.complex128)
     p = oracle.make_params(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"],
                            PARAMS["beta"], PARAMS["gamma0"], PARAMS["gamma2"], dealias=PARAMS["dealias"])
     t = time.perf_counter()
-    oracle.run(p, w0, (0.0, 0.0), nsteps, "f32", nthreads=threads)
+    oracle.run(p, w0, (0.0, 0.0), nsteps, "f32" if PRECISION == "fp32" else "f64", nthreads=threads)
     return time.perf_counter() - t, oracle.num_threads() if threads == 0 else threads
 
 
@@ -155,9 +179,10 @@ def run_ours(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     sim = am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"], PARAMS["beta"],
-                    gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"], precision="fp32")
+                    gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"], precision=PRECISION)
     sim.set_stream(stream.cuda_stream)
-    w0 = am.ic_bandlimited(NX, NY, SEED).astype(np.complex64)
+    cdt = np.complex64 if PRECISION == "fp32" else np.complex128
+    w0 = am.ic_bandlimited(NX, NY, SEED).astype(cdt)
     sim.set_state(w0, (0.0, 0.0))
 
     # warm-up
@@ -196,7 +221,7 @@ def run_ours(args):
     H = NY * (NX // 2 + 1)                 # half-plane values per field
     kxc = sim.kx_carried                   # Nx/4 with pruned transforms, Nx/2 without
     Hc = NY * (kxc + 1)                    # values per field the passes move
-    s = 8
+    s = 8 if PRECISION == "fp32" else 16
     row_avg = row.sum() / (4 * nprof)
     col_avg = col.sum() / (4 * nprof)
     # algorithmic bytes per launch: row pass 5 fields (3 in, 2 out); column
@@ -205,18 +230,19 @@ def run_ours(args):
     col_bytes = 7.5 * s * Hc
     peak, peak_kind = peaks()
     if col.sum() >= row.sum():
-        dom, dom_bytes, dom_ms = "column pass (FFT_y, stage update, Biot-Savart, IFFT_y)", col_bytes, col_avg
+        dom, dom_bytes, dom_ms, key = "column pass (FFT_y, stage update, Biot-Savart, IFFT_y)", col_bytes, col_avg, "col"
     else:
-        dom, dom_bytes, dom_ms = "row pass (C2R_x, products, R2C_x)", row_bytes, row_avg
+        dom, dom_bytes, dom_ms, key = "row pass (C2R_x, products, R2C_x)", row_bytes, row_avg, "row"
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
     step_bytes = 50 * s * Hc
     step_achieved = step_bytes / (total_ms / args.steps / 1e3) / 1e9
     full_step_achieved = 50 * s * H / (total_ms / args.steps / 1e3) / 1e9
 
     # ---- e2e through the C ABI with host buffers (pinned)
-    w_host = torch.empty((NY, NX // 2 + 1), dtype=torch.complex64, pin_memory=True)
+    tdt = torch.complex64 if PRECISION == "fp32" else torch.complex128
+    w_host = torch.empty((NY, NX // 2 + 1), dtype=tdt, pin_memory=True)
     w_host.numpy()[:] = w0
-    w_out = torch.empty((NY, NX // 2 + 1), dtype=torch.complex64, pin_memory=True)
+    w_out = torch.empty((NY, NX // 2 + 1), dtype=tdt, pin_memory=True)
     e_out = torch.empty(args.steps, dtype=torch.float64, pin_memory=True)
     wh, wo, eo = w_host.numpy(), w_out.numpy(), e_out.numpy()
     import ctypes
@@ -236,7 +262,7 @@ def run_ours(args):
 
     # ---- CPU baseline: the oracle on the host cores, bounded sample
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and PRECISION == "fp32":
         n_cpu = 0
         t_cpu = 0.0
         cores = 1
@@ -251,12 +277,12 @@ def run_ours(args):
     out = {
         "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "dt": PARAMS["dt"], "dealias": "half",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if PRECISION == "fp32" else "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "dt": PARAMS["dt"], "dealias": PARAMS["dealias"],
                    "parallelism": "single GPU", "l2": "flushed before every timed step (256 MB write)",
                    "timing": "CUDA events on the solver stream, one CUDA graph (8 kernels) per step"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": dom, "algorithmic_bytes_per_launch": dom_bytes,
+                     "traffic": NCU_TRAFFIC[key] if (NX == 2048 and PRECISION == "fp32" and kxc == NX // 4) else None, "kernel": dom, "algorithmic_bytes_per_launch": dom_bytes,
                      "avg_launch_ms": dom_ms, "peak_source": peak_kind,
                      "row_pass_ms": row_avg, "column_pass_ms": col_avg,
                      "step_achieved_gbs": step_achieved, "step_frac": step_achieved / peak,
@@ -273,6 +299,62 @@ def run_ours(args):
     print(json.dumps(out), flush=True)
 
 
+def run_accuracy(args):
+    """Precision form: FP32 against the FP64 path from the same seeded field.
+
+    Short horizon: relative L2 of w_hat after 200 steps.  Long horizon: the
+    time-mean energy over the second half of the run and the time-averaged
+    shell spectrum (snapshots every 1000 steps in the second half).  The FP64
+    path is the solver's own double-precision build, which agrees with the
+    CPU FP64 oracle to 1e-10 over the parity tests' horizons."""
+    import importlib
+
+    import numpy as np
+
+    am = importlib.import_module("2d_active_matter_simulation_gb300")
+    spec = importlib.import_module("2d_active_matter_simulation_gb300.spectrum")
+    n_total = args.acc_steps
+    w0 = am.ic_bandlimited(NX, NY, SEED)
+    res = {}
+    runs = {}
+    for prec in ("fp32", "fp64"):
+        sim = am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"],
+                        PARAMS["beta"], gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"],
+                        dealias=PARAMS["dealias"], precision=prec)
+        sim.set_state(w0 if prec == "fp64" else w0.astype(np.complex64))
+        t0 = time.perf_counter()
+        e = [sim.step(200)]
+        w200, _ = sim.get_state()
+        specs = []
+        done = 200
+        while done < n_total:
+            k = min(1000, n_total - done)
+            e.append(sim.step(k))
+            done += k
+            if done >= n_total // 2:
+                w, m = sim.get_state()
+                specs.append(spec.energy_spectrum(w.astype(np.complex128), m, NX, NY, PARAMS["lx"], PARAMS["ly"])[1])
+        dt_run = time.perf_counter() - t0
+        sim.close()
+        runs[prec] = dict(w200=w200.astype(np.complex128), energy=np.concatenate(e),
+                          spec=np.mean(specs, axis=0) if specs else None, seconds=dt_run)
+    a, b = runs["fp32"], runs["fp64"]
+    half = len(b["energy"]) // 2
+    res["short_horizon_steps"] = 200
+    res["w_rel_l2_200"] = float(np.linalg.norm(a["w200"] - b["w200"]) / np.linalg.norm(b["w200"]))
+    res["long_horizon_steps"] = n_total
+    res["mean_energy_fp32"] = float(np.mean(a["energy"][half:]))
+    res["mean_energy_fp64"] = float(np.mean(b["energy"][half:]))
+    res["mean_energy_rel_diff"] = abs(res["mean_energy_fp32"] / res["mean_energy_fp64"] - 1)
+    if a["spec"] is not None:
+        kmax = NX // 4   # shells carried by the 1/2 rule
+        res["spectrum_max_rel_diff"] = spec.spectrum_rel_error(a["spec"], b["spec"], kmax)
+    res["seconds_fp32"] = a["seconds"]
+    res["seconds_fp64"] = b["seconds"]
+    res["gps_fp64"] = NX * NY * n_total / b["seconds"]
+    print(json.dumps({"accuracy": res, "config": {"workload": WORKLOAD}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -280,7 +362,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--accuracy", action="store_true", help="FP32 vs FP64 precision-form check instead")
+    ap.add_argument("--acc-steps", type=int, default=20000)
+    ap.add_argument("--config", type=int, default=1, choices=sorted(PRESETS))
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     args = ap.parse_args()
+    apply_preset(args.config, args.precision)
+    if args.accuracy:
+        run_accuracy(args)
+        return
     if args.gpus != 1:
         if int(os.environ.get("RANK", "0")) == 0:
             print(json.dumps({"error": "this solver runs one simulation per GPU; replicas are independent, "

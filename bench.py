@@ -304,7 +304,8 @@ def run_accuracy(args):
 
     Short horizon: relative L2 of w_hat after 200 steps.  Long horizon: the
     time-mean energy over the second half of the run and the time-averaged
-    shell spectrum (snapshots every 1000 steps in the second half).  The FP64
+    shell spectrum (snapshots every 200 steps in the second half; the flow is
+    chaotic, so the spectra agree only statistically).  The FP64
     path is the solver's own double-precision build, which agrees with the
     CPU FP64 oracle to 1e-10 over the parity tests' horizons."""
     import importlib
@@ -328,7 +329,7 @@ def run_accuracy(args):
         specs = []
         done = 200
         while done < n_total:
-            k = min(1000, n_total - done)
+            k = min(200, n_total - done)
             e.append(sim.step(k))
             done += k
             if done >= n_total // 2:
@@ -349,6 +350,9 @@ def run_accuracy(args):
     if a["spec"] is not None:
         kmax = NX // 4   # shells carried by the 1/2 rule
         res["spectrum_max_rel_diff"] = spec.spectrum_rel_error(a["spec"], b["spec"], kmax)
+        sa, sb = a["spec"][: kmax + 1], b["spec"][: kmax + 1]
+        res["spectrum_l1_rel_diff"] = float(np.sum(np.abs(sa - sb)) / np.sum(sb))
+        res["spectrum_snapshots"] = (n_total - n_total // 2) // 200
     res["seconds_fp32"] = a["seconds"]
     res["seconds_fp64"] = b["seconds"]
     res["gps_fp64"] = NX * NY * n_total / b["seconds"]

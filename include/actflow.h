@@ -117,6 +117,24 @@ am_status am_sync(am_handle *h);
  * For measurement; am_step is the production path (one CUDA graph per step). */
 am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double col_ms[4]);
 
+/* Advance nsteps steps without allocating anything.  No counterpart in the
+ * reference: it exists for callers that may not allocate device memory -- a
+ * plug-in whose host application owns the device-memory budget, or a real-time
+ * loop that cannot take cudaMalloc's synchronisation and latency.  All buffers
+ * are the caller's and live in device memory: w_hat [Ny][Nx/2+1] complex of the
+ * precision in p (read, then overwritten with the new state), mean[2] (scaled
+ * mean velocity, read and overwritten), energy[nsteps] (energy of the state
+ * entering each step) or NULL.  Every intermediate buffer comes from one
+ * library-owned device array of 8 MiB (held by every GPU that loads the
+ * library until the process exits): grids whose scratch does not fit -- larger
+ * than 512^2 in FP32 or 512x256 in FP64 -- are refused with AM_ERR_UNSUPPORTED.
+ * The first call on a device looks up that array's device address (do it before
+ * any stream capture).  The work is enqueued on `stream` (a cudaStream_t, NULL =
+ * default stream) and the call returns without waiting; it runs the full
+ * transforms and reports no NaN (check mean or the energies).  Calls share the
+ * array: calls that overlap on the GPU race and must be serialised. */
+am_status am_step_noalloc(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy, void *stream);
+
 /* Number of kernel launches one step makes (for accounting). */
 int am_launches_per_step(const am_handle *h);
 

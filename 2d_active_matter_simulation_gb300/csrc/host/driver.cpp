@@ -23,6 +23,7 @@
 #include <fstream>
 #include <iostream>
 #include <random>
+#include <thread>
 #include <vector>
 
 #include "host.h"
@@ -46,7 +47,8 @@ const char *HELP =
     "  initial_condition (random [n] | blank | continue [T_ext [snapshot]] |\n"
     "                     bandlimited <seed> [kmin kmax rms]),\n"
     "  save_directory,\n"
-    "  optional: precision (fp32|fp64), dealias (reference|half|none), Gamma0, Gamma2\n"
+    "  optional: precision (fp32|fp64), dealias (reference|half|none), Gamma0, Gamma2,\n"
+    "            snapshot_binary (1: exact ActTurb_snap{i}.raw beside each snapshot)\n"
     "--------------------------------------------------\n";
 
 int write_default_spec()
@@ -105,6 +107,61 @@ bool exists(const std::string &path)
 }
 
 std::string snap_path(const std::string &dir, long long i) { return dir + "/ActTurb_snap" + std::to_string(i) + ".bin"; }
+std::string raw_path(const std::string &dir, long long i) { return dir + "/ActTurb_snap" + std::to_string(i) + ".raw"; }
+
+// Snapshots without stalling the step loop.  The file is opened on the calling
+// thread (so an unwritable directory fails at the same step as in the
+// reference, ActFlow_V3-2.cu:824-839), the state is copied to one of two host
+// buffers, and a background thread formats and writes the text (the slow part
+// at large grids) while the GPU runs the next steps.  A second snapshot waits
+// for the first writer to finish before reusing its buffer.
+class SnapshotWriter {
+  public:
+    SnapshotWriter(int nx, int ny, bool fp64, bool raw, size_t bytes) : nx_(nx), ny_(ny), fp64_(fp64), raw_(raw)
+    {
+        buf_[0].resize(bytes);
+        buf_[1].resize(bytes);
+    }
+    ~SnapshotWriter() { finish(); }
+    // Buffer the next snapshot's state goes into.
+    void *buffer() { return buf_[cur_].data(); }
+    double *mean() { return mean_[cur_]; }
+    // Hand the current buffer to the writer thread.  False if the file cannot
+    // be created or an earlier write failed.
+    bool submit(const std::string &dir, long long index)
+    {
+        std::FILE *f = std::fopen(snap_path(dir, index).c_str(), "wb");
+        if (!f) return false;
+        if (!finish()) {
+            std::fclose(f);
+            return false;
+        }
+        const int b = cur_;
+        const std::string rp = raw_ ? raw_path(dir, index) : std::string();
+        th_ = std::thread([this, f, b, rp]() {
+            bool ok = write_snapshot_to(f, nx_, ny_, fp64_, buf_[b].data(), mean_[b]);
+            if (!rp.empty()) ok = write_snapshot_raw(rp, nx_, ny_, fp64_, buf_[b].data(), mean_[b]) && ok;
+            ok_ = ok;
+        });
+        cur_ ^= 1;
+        return true;
+    }
+    // Wait for the writer; false if its write failed.
+    bool finish()
+    {
+        if (th_.joinable()) th_.join();
+        return ok_;
+    }
+
+  private:
+    int nx_, ny_;
+    bool fp64_, raw_;
+    std::vector<unsigned char> buf_[2];
+    double mean_[2][2] = {{0, 0}, {0, 0}};
+    int cur_ = 0;
+    std::thread th_;
+    bool ok_ = true;
+};
 
 }  // namespace
 
@@ -260,7 +317,11 @@ int cli_main(int argc, char **argv)
         }
         std::cout << "continue execution from snapshot " << cont << std::endl;
         m = cont * snap;
-        if (!read_snapshot(snap_path(dir, cont), s.Nx, s.Ny, fp64, w.data(), mean)) {
+        // An exact binary sidecar of the same snapshot, when present, is used
+        // instead of the six-digit text.
+        if (read_snapshot_raw(raw_path(dir, cont), s.Nx, s.Ny, fp64, w.data(), mean)) {
+            std::cout << "using the exact binary copy " << raw_path(dir, cont) << std::endl;
+        } else if (!read_snapshot(snap_path(dir, cont), s.Nx, s.Ny, fp64, w.data(), mean)) {
             std::cerr << "Error: unable to open previous simulation" << std::endl;
             return 1;
         }
@@ -273,12 +334,12 @@ int cli_main(int argc, char **argv)
         std::cerr << "Error: " << am_status_string(st) << ": " << am_last_error(h) << std::endl;
         return 1;
     }
+    SnapshotWriter writer(s.Nx, s.Ny, fp64, s.snapshot_binary, w.size());
     if (m == 1) {
         // A fresh start saves the processed initial condition as snapshot 0
         // (ActFlow_V3-2.cu:660-694).
         std::cout << "processing the initial condition" << std::endl;
-        if ((st = am_get_state(h, w.data(), mean)) ||
-            !write_snapshot(snap_path(dir, 0), s.Nx, s.Ny, fp64, w.data(), mean)) {
+        if ((st = am_get_state(h, writer.buffer(), writer.mean())) || !writer.submit(dir, 0)) {
             std::cerr << "Error: unable to create snapshot file" << std::endl;
             return 1;
         }
@@ -309,22 +370,27 @@ int cli_main(int argc, char **argv)
         long long m_end = m + good - 1;
         bool at_snap = m_end % snap == 0 && (st != AM_ERR_NAN || good == k);
         if (at_snap) {
-            if (am_get_state(h, w.data(), mean) ||
-                !write_snapshot(snap_path(dir, m_end / snap), s.Nx, s.Ny, fp64, w.data(), mean)) {
+            const void *sw = writer.buffer();
+            if (am_get_state(h, writer.buffer(), writer.mean()) || !writer.submit(dir, m_end / snap)) {
                 std::cerr << "Error: unable to create snapshot file" << std::endl;
                 return 1;
             }
             std::chrono::duration<double> el = std::chrono::high_resolution_clock::now() - t0;
-            double w0r = fp64 ? ((double *)w.data())[0] : ((float *)w.data())[0];
-            double w0i = fp64 ? ((double *)w.data())[1] : ((float *)w.data())[1];
+            double w0r = fp64 ? ((const double *)sw)[0] : ((const float *)sw)[0];
+            double w0i = fp64 ? ((const double *)sw)[1] : ((const float *)sw)[1];
             std::cout << "\r" << m_end << " / " << M << " timesteps done in " << el.count() << "s, w[0]=("
                       << fmt_g(w0r) << "," << fmt_g(w0i) << ")    " << std::flush;
         }
         if (st == AM_ERR_NAN) {
+            writer.finish();
             std::cerr << "\nError: array contains nan values after " << m_end << " timesteps" << std::endl;
             return 1;
         }
         m = last + 1;
+    }
+    if (!writer.finish()) {
+        std::cerr << "Error: unable to create snapshot file" << std::endl;
+        return 1;
     }
     std::chrono::duration<double> el = std::chrono::high_resolution_clock::now() - t0;
     std::cout << "\nprogram finished successfully after " << el.count() << "s.\n" << std::endl;

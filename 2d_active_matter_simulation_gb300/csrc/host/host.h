@@ -1,6 +1,7 @@
 // Host-side front end of the actflow solver: the reference program's process
 // contract (specifications.txt, snapshot and energy files, command line).
 #pragma once
+#include <cstdio>
 #include <string>
 #include <vector>
 
@@ -29,6 +30,7 @@ struct Spec {
     double gamma0 = 0.0, gamma2 = 0.0;
     int precision = AM_FP32;
     int dealias = AM_DEALIAS_REFERENCE;
+    bool snapshot_binary = false;   // also write the exact binary sidecar ActTurb_snap{i}.raw
 };
 
 // Read <dir>/specifications.txt into `s` (which holds the defaults on entry).
@@ -40,6 +42,14 @@ int read_spec(const std::string &dir, Spec &s, std::string &err);
 // default ostream format (six significant digits), ActFlow_V3-2.cu:1261-1263.
 // `fp64` selects double values (else float).
 bool write_snapshot(const std::string &path, int nx, int ny, bool fp64, const void *w_hat, const double mean[2]);
+// Format and write a snapshot into an already opened file, then close it.
+bool write_snapshot_to(std::FILE *f, int nx, int ny, bool fp64, const void *w_hat, const double mean[2]);
+// Exact binary sidecar: "AFRAW1" magic, nx, ny, precision, the raw half-plane
+// values and the mean in double.  Lets `continue` resume bit for bit (the text
+// keeps six significant digits, ActFlow_V3-2.cu:1262).
+bool write_snapshot_raw(const std::string &path, int nx, int ny, bool fp64, const void *w_hat, const double mean[2]);
+// Returns false if absent or not matching (nx, ny, precision).
+bool read_snapshot_raw(const std::string &path, int nx, int ny, bool fp64, void *w_hat, double mean[2]);
 // Parse a snapshot back (continue path, ActFlow_V3-2.cu:620-631).  Returns
 // false if the file cannot be opened or holds fewer numbers than needed.
 bool read_snapshot(const std::string &path, int nx, int ny, bool fp64, void *w_hat, double mean[2]);

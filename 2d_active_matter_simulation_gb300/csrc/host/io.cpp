@@ -21,9 +21,45 @@ std::string fmt_g(double v)
 
 bool write_snapshot(const std::string &path, int nx, int ny, bool fp64, const void *w_hat, const double mean[2])
 {
-    const size_t n = (size_t)ny * (nx / 2 + 1);
     std::FILE *f = std::fopen(path.c_str(), "wb");
     if (!f) return false;
+    return write_snapshot_to(f, nx, ny, fp64, w_hat, mean);
+}
+
+namespace {
+const char kRawMagic[8] = {'A', 'F', 'R', 'A', 'W', '1', 0, 0};
+}
+
+bool write_snapshot_raw(const std::string &path, int nx, int ny, bool fp64, const void *w_hat, const double mean[2])
+{
+    std::FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) return false;
+    const int hdr[4] = {nx, ny, fp64 ? AM_FP64 : AM_FP32, 0};
+    const size_t n = (size_t)ny * (nx / 2 + 1) * 2;
+    bool ok = std::fwrite(kRawMagic, 1, 8, f) == 8 && std::fwrite(hdr, sizeof(int), 4, f) == 4 &&
+              std::fwrite(w_hat, fp64 ? 8 : 4, n, f) == n && std::fwrite(mean, sizeof(double), 2, f) == 2;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok;
+}
+
+bool read_snapshot_raw(const std::string &path, int nx, int ny, bool fp64, void *w_hat, double mean[2])
+{
+    std::FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) return false;
+    char magic[8];
+    int hdr[4];
+    const size_t n = (size_t)ny * (nx / 2 + 1) * 2;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kRawMagic, 8) == 0 &&
+              std::fread(hdr, sizeof(int), 4, f) == 4 && hdr[0] == nx && hdr[1] == ny &&
+              hdr[2] == (fp64 ? AM_FP64 : AM_FP32) && std::fread(w_hat, fp64 ? 8 : 4, n, f) == n &&
+              std::fread(mean, sizeof(double), 2, f) == 2;
+    std::fclose(f);
+    return ok;
+}
+
+bool write_snapshot_to(std::FILE *f, int nx, int ny, bool fp64, const void *w_hat, const double mean[2])
+{
+    const size_t n = (size_t)ny * (nx / 2 + 1);
     std::vector<char> out;
     out.reserve(n * 26 + 64);
     char buf[64];

@@ -7,6 +7,7 @@
 //   precision:  fp32 | fp64
 //   dealias:    reference | half | none
 //   Gamma0:, Gamma2:  select the general linear operator -alpha - G0 k^2 - G2 k^4
+//   snapshot_binary:  1 = also write ActTurb_snap{i}.raw (exact, used by continue)
 #include <fstream>
 #include <stdexcept>
 
@@ -85,6 +86,11 @@ int read_spec(const std::string &dir, Spec &s, std::string &err)
             else if (val == "half") s.dealias = AM_DEALIAS_HALF;
             else if (val == "none") s.dealias = AM_DEALIAS_NONE;
             else ok = false;
+        } else if (line == "snapshot_binary:") {
+            next();
+            int b = 0;
+            ok = to_int(val, b);
+            s.snapshot_binary = b != 0;
         } else if (line == "Gamma0:") {
             next();
             ok = to_double(val, s.gamma0);

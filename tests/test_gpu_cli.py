@@ -100,3 +100,59 @@ def test_cli_fresh_bandlimited_fp64(am, tmp_path):
     t, e = read_energy(os.path.join(d, "energy.txt"))
     assert len(t) == 10 and abs(t[0] - 0.001) < 1e-9
     assert os.path.exists(os.path.join(d, "ActTurb_snap2.bin"))
+
+
+def _raw(path, nx, ny):
+    with open(path, "rb") as f:
+        b = f.read()
+    assert b[:6] == b"AFRAW1"
+    hdr = np.frombuffer(b[8:24], dtype=np.int32)
+    assert tuple(hdr[:2]) == (nx, ny)
+    n = ny * (nx // 2 + 1)
+    w = np.frombuffer(b[24:24 + 8 * n], dtype=np.complex64).reshape(ny, nx // 2 + 1)
+    m = np.frombuffer(b[24 + 8 * n:], dtype=np.float64)
+    return w, m
+
+
+def test_cli_binary_sidecar_resumes_exactly(am, tmp_path):
+    """snapshot_binary: 1 writes ActTurb_snap{i}.raw beside each text snapshot;
+    `continue` then resumes from the exact state (the text has six digits)."""
+    nx = ny = 64
+    d = str(tmp_path)
+    spec = [("T", "0.05"), ("dt", "0.005"), ("Lx", "50.26548"), ("Ly", "50.26548"), ("Nx", nx), ("Ny", ny),
+            ("lambda", "7"), ("alpha", "-0.8"), ("beta", "0.01"), ("dt_snap", "0.025"),
+            ("initial_condition", "bandlimited 5 1 8 1.0"), ("save_directory", d), ("snapshot_binary", "1")]
+    write_spec(os.path.join(d, "specifications.txt"), spec)
+    p = _run(am, d)
+    assert p.returncode == 0, p.stderr
+    for i in range(3):
+        w_txt, m_txt = read_snapshot(os.path.join(d, f"ActTurb_snap{i}.bin"), nx, ny)
+        w_raw, m_raw = _raw(os.path.join(d, f"ActTurb_snap{i}.raw"), nx, ny)
+        assert np.allclose(w_txt, w_raw, rtol=1e-5, atol=1e-6 * np.abs(w_raw).max())
+    # resume from snapshot 1 (m = 5, steps 5..10 -> 6 steps, the reference's numbering)
+    w1, m1 = _raw(os.path.join(d, "ActTurb_snap1.raw"), nx, ny)
+    for f in ("ActTurb_snap2.bin", "ActTurb_snap2.raw", "energy.txt"):
+        os.remove(os.path.join(d, f))
+    spec[10] = ("initial_condition", "continue")
+    write_spec(os.path.join(d, "specifications.txt"), spec)
+    p = _run(am, d)
+    assert p.returncode == 0, p.stderr
+    assert "exact binary copy" in p.stdout
+    w2, m2 = _raw(os.path.join(d, "ActTurb_snap2.raw"), nx, ny)
+    sim = am.Solver(nx, ny, float(np.float32(50.26548)), float(np.float32(50.26548)), float(np.float32(0.005)),
+                    7.0, float(np.float32(-0.8)), float(np.float32(0.01)))
+    sim.set_state(w1, m1)
+    sim.step(6)
+    w, m = sim.get_state()
+    sim.close()
+    assert np.array_equal(w, w2) and np.array_equal(m, m2)
+
+
+def test_cli_unwritable_snapshot_dir_exits_1(am, tmp_path):
+    d = str(tmp_path)
+    out = os.path.join(d, "no", "such", "dir")
+    write_spec(os.path.join(d, "specifications.txt"), [
+        ("T", "0.01"), ("dt", "0.005"), ("Nx", 32), ("Ny", 32), ("Lx", "30"), ("Ly", "30"),
+        ("initial_condition", "blank"), ("save_directory", out)])
+    p = _run(am, d)
+    assert p.returncode == 1 and "unable to create snapshot file" in p.stderr

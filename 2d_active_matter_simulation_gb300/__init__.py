@@ -89,6 +89,12 @@ def _load():
         "am_append_energy": ([ctypes.c_char_p, ctypes.c_longlong, ctypes.c_int, ctypes.c_float, dp,
                               ctypes.c_int], ctypes.c_int),
         "am_cli_main": ([ctypes.c_int, ctypes.POINTER(ctypes.c_char_p)], ctypes.c_int),
+        "am_batch_create": ([ctypes.POINTER(Params), ctypes.c_int, ctypes.POINTER(hp)], ctypes.c_int),
+        "am_batch_destroy": ([hp], ctypes.c_int),
+        "am_batch_set_state": ([hp, ctypes.c_int, vp, dp], ctypes.c_int),
+        "am_batch_get_state": ([hp, ctypes.c_int, vp, dp], ctypes.c_int),
+        "am_batch_step": ([hp, ctypes.c_int, dp, ip], ctypes.c_int),
+        "am_batch_last_error": ([hp], ctypes.c_char_p),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -105,7 +111,8 @@ EXPORTED = [
     "am_step", "am_step_async", "am_sync", "am_step_profiled", "am_step_noalloc", "am_launches_per_step", "am_device_bytes", "am_kx_carried",
     "am_status_string",
     "am_last_error", "am_mask_value", "am_ic_bandlimited", "am_spec_read", "am_write_snapshot",
-    "am_read_snapshot", "am_append_energy", "am_cli_main",
+    "am_read_snapshot", "am_append_energy", "am_cli_main", "am_batch_create", "am_batch_destroy",
+    "am_batch_set_state", "am_batch_get_state", "am_batch_step", "am_batch_last_error",
 ]
 
 
@@ -207,6 +214,59 @@ class Solver:
     @property
     def device_bytes(self):
         return lib.am_device_bytes(self.h)
+
+
+class Batch:
+    """An ensemble of simulations of one grid advanced together (am_batch)."""
+
+    def __init__(self, params_list):
+        n = len(params_list)
+        arr = (Params * n)(*params_list)
+        self.nx, self.ny, self.n = params_list[0].nx, params_list[0].ny, n
+        self.h = ctypes.c_void_p()
+        _check(lib.am_batch_create(arr, n, ctypes.byref(self.h)), None, "am_batch_create")
+
+    def _chk(self, st, what):
+        if st != AM_OK:
+            raise ActflowError(st, f"{what}: {status_string(st)} {lib.am_batch_last_error(self.h).decode()}")
+
+    def close(self):
+        if self.h:
+            lib.am_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, member, w_hat, mean=(0.0, 0.0)):
+        w = np.ascontiguousarray(w_hat, dtype=np.complex64)
+        m = np.array(mean, dtype=np.float64)
+        self._chk(lib.am_batch_set_state(self.h, member, w.ctypes.data, _dptr(m)), "am_batch_set_state")
+
+    def get_state(self, member):
+        w = np.zeros((self.ny, self.nx // 2 + 1), dtype=np.complex64)
+        m = np.zeros(2)
+        self._chk(lib.am_batch_get_state(self.h, member, w.ctypes.data, _dptr(m)), "am_batch_get_state")
+        return w, m
+
+    def step(self, nsteps, energy=True):
+        e = np.zeros((max(nsteps, 1), self.n))
+        nan_m = ctypes.c_int(-1)
+        st = lib.am_batch_step(self.h, nsteps, _dptr(e) if energy else None, ctypes.byref(nan_m))
+        self._chk(st, "am_batch_step")
+        return e[:nsteps]
+
+
+def make_params(nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None, dealias="reference",
+                precision="fp32"):
+    form = FORM_REFERENCE if gamma0 is None else FORM_GENERAL
+    return Params(nx, ny, lx, ly, dt, lam, alpha, beta, 0.0 if gamma0 is None else gamma0,
+                  0.0 if gamma2 is None else gamma2, form,
+                  DEALIAS[dealias] if isinstance(dealias, str) else int(dealias),
+                  FP64 if precision in ("fp64", FP64) else FP32)
 
 
 def mask_value(nx, ny, dealias, ix, iy):

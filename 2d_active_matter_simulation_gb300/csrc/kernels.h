@@ -34,4 +34,17 @@ struct KernelTable {
 const KernelTable<float> &kernels_f32();
 const KernelTable<double> &kernels_f64();
 
+// Batched forms of the step kernels: one launch covers every member of an
+// ensemble (blockIdx.y = member), each member's arguments read from a device
+// array.  FP32, grids 128..1024 per axis.
+constexpr int BATCH_LOG_MIN = 7;
+constexpr int BATCH_LOG_MAX = 10;
+
+struct BatchTable {
+    void (*row[LOG_MAX + 1])(const StepArgs<float> *);
+    void (*col[LOG_MAX + 1][5])(const StepArgs<float> *);
+};
+
+const BatchTable &kernels_batch_f32();
+
 }  // namespace af

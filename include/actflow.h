@@ -135,6 +135,25 @@ am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double co
  * array: calls that overlap on the GPU race and must be serialised. */
 am_status am_step_noalloc(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy, void *stream);
 
+/* ------------------------------------------------------------ ensembles --
+ * A batch advances B simulations of one grid with the same launches (each pass
+ * is one launch over all members, a step one CUDA graph).  The reference runs
+ * one simulation per process; a batch is that loop (ActFlow_V3-2.cu:718-862)
+ * for B independent states at once.  All members share nx, ny, lx, ly, dt,
+ * form and dealias; lambda, alpha, beta, gamma0, gamma2 may differ.  FP32,
+ * grids 128..1024 per axis.  Each member computes exactly what a handle with
+ * its parameters computes. */
+typedef struct am_batch am_batch;
+am_status am_batch_create(const am_params *params /* [nmembers] */, int nmembers, am_batch **out);
+am_status am_batch_destroy(am_batch *b);
+/* Member state in and out, as am_set_state / am_get_state (host buffers). */
+am_status am_batch_set_state(am_batch *b, int member, const void *w_hat, const double mean[2]);
+am_status am_batch_get_state(am_batch *b, int member, void *w_hat, double mean[2]);
+/* nsteps steps for every member; energy, if not NULL, receives [nsteps][B]
+ * values.  AM_ERR_NAN names the first member whose w(0,0) became NaN. */
+am_status am_batch_step(am_batch *b, int nsteps, double *energy, int *nan_member);
+const char *am_batch_last_error(const am_batch *b);
+
 /* Number of kernel launches one step makes (for accounting). */
 int am_launches_per_step(const am_handle *h);
 

@@ -374,6 +374,80 @@ struct BlockFFT {
     }
 
     static constexpr int ipow(int b, int p) { return p == 0 ? 1 : b * ipow(b, p - 1); }
+
+    // NF transforms of the same length and direction in lockstep: v[f] holds
+    // transform f (cyclic distribution), b0[f] / b1[f] are its two exchange
+    // buffers.  The twiddles of a pass are formed once for all NF transforms
+    // and one barrier per exchange serves all of them, and the NF independent
+    // DFTs per thread give the scheduler more work between shared-memory
+    // accesses.
+    template <int NF, class Buf, class Sync>
+    static AF_HD void run_multi(cpx<T> (&v)[NF][R], int j, int c, const Buf (&b0)[NF], const Buf (&b1)[NF],
+                                const cpx<T> *tw, int TWS, Sync &&sync)
+    {
+        if constexpr (NEXCH > 0) sync();
+        int e = 0;
+        if constexpr (LOGR1 > 0) {
+            constexpr int G = R / R1;
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+#pragma unroll
+                for (int q = 0; q < G; q++) {
+                    cpx<T> u[R1];
+#pragma unroll
+                    for (int r1 = 0; r1 < R1; r1++) u[r1] = v[f][q + G * r1];
+                    DFT<R1, SIGN, T>::run(u);
+                    const int base = (j + q * TPC) * R1;
+#pragma unroll
+                    for (int r1 = 0; r1 < R1; r1++) b0[f].d[b0[f].template at<1>(base, r1, c)] = u[r1];
+                }
+            }
+            sync();
+            e = 1;
+        }
+        pass_multi<0, LOGR1 == 0, NF>(v, j, c, b0, b1, tw, TWS, sync, e);
+    }
+
+    template <int P, bool FROM_REGS, int NF, class Buf, class Sync>
+    static AF_HD void pass_multi(cpx<T> (&v)[NF][R], int j, int c, const Buf (&b0)[NF], const Buf (&b1)[NF],
+                                 const cpx<T> *tw, int TWS, Sync &&sync, int e)
+    {
+        if constexpr (P < NPASS) {
+            constexpr int NS = R1 * ipow(R, P);
+            if constexpr (!FROM_REGS) {
+#pragma unroll
+                for (int f = 0; f < NF; f++) {
+                    const Buf &b = ((e & 1) == 1) ? b0[f] : b1[f];   // written by exchange e-1
+#pragma unroll
+                    for (int r = 0; r < R; r++) v[f][r] = b.d[b.template at<TPC>(j, r, c)];
+                }
+            }
+            if constexpr (NS > 1) {
+                const int k = j & (NS - 1);
+                const int step = (L / (NS * R)) * k * TWS;
+                cpx<T> w[R];
+                twiddles<R>(w, tw, step);
+#pragma unroll
+                for (int f = 0; f < NF; f++)
+#pragma unroll
+                    for (int r = 1; r < R; r++) v[f][r] = SIGN < 0 ? cmul(v[f][r], w[r]) : cmulc(v[f][r], w[r]);
+            }
+#pragma unroll
+            for (int f = 0; f < NF; f++) DFT<R, SIGN, T>::run(v[f]);
+            if constexpr (P < NPASS - 1) {
+                const int k = j & (NS - 1);
+                const int base = (j - k) * R + k;
+#pragma unroll
+                for (int f = 0; f < NF; f++) {
+                    const Buf &b = ((e & 1) == 0) ? b0[f] : b1[f];
+#pragma unroll
+                    for (int r = 0; r < R; r++) b.d[b.template at<NS>(base, r, c)] = v[f][r];
+                }
+                sync();
+                pass_multi<P + 1, false, NF>(v, j, c, b0, b1, tw, TWS, sync, e + 1);
+            }
+        }
+    }
 };
 
 }  // namespace af

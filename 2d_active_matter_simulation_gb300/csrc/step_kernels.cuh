@@ -156,8 +156,10 @@ struct RowPass {
     using Buf = XBuf<T, 1, sizeof(T) == 4 ? 1 : 2>;
     static constexpr int BUFS = (Buf::slots(M) + 7) / 8 * 8;   // complex slots per buffer
 
-    // two exchange buffers per row (double buffering)
-    static constexpr size_t smem_bytes() { return (size_t)ROWS * 2 * BUFS * sizeof(cpx<T>); }
+    // per row: two exchange buffers (double buffering) for each of the three
+    // transforms that run in lockstep
+    static constexpr int NBUF = 6;
+    static constexpr size_t smem_bytes() { return (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>); }
 
     // C2R pre-processing of X(k), X(M-k): Z(k) = E + i O with
     // E = X(k) + conj X(M-k), O = (X(k) - conj X(M-k)) exp(2 pi i k / Nx).
@@ -323,57 +325,42 @@ struct RowPass {
         const bool active = yy < a.ny;
         const int y = active ? yy : a.ny - 1;   // inactive rows recompute the last row, never store
         const int ny = a.ny;
-        Buf b0{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * 2 * BUFS};
-        Buf b1{reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * 2 * BUFS + BUFS};
+        cpx<T> *rbase = reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * NBUF * BUFS;
+        const Buf b0[3] = {Buf{rbase}, Buf{rbase + BUFS}, Buf{rbase + 2 * BUFS}};
+        const Buf b1[3] = {Buf{rbase + 3 * BUFS}, Buf{rbase + 4 * BUFS}, Buf{rbase + 5 * BUFS}};
 
-        // ---- C2R along x of uy, ux (kept) and w (consumed by the products).
-        // The Hermitian pairs of the next field are loaded before the current
-        // field's transform, so their latency overlaps the FFT.
+        // ---- C2R along x of uy, ux and w, the three transforms in lockstep
         const cpx<T> wj = ldtw(a.twx, j);
-        cpx<T> zy[R], zx[R], v[R];
-        {
-            cpx<T> A[R], B[R];
-            load_pairs(A, B, a.fy, j, y, ny, a.kxp);
-            pack_pairs(v, A, B, wj, j);
-        }
-        FFTi::run(v, j, 0, b0, b1, a.twx, 2, sync);
+        cpx<T> v[3][R];
+        const cpx<T> *src[3] = {a.fy, a.fx, a.fa};
 #pragma unroll
-        for (int r = 0; r < R; r++) zy[r] = v[r];
-        {
+        for (int f = 0; f < 3; f++) {
             cpx<T> A[R], B[R];
-            load_pairs(A, B, a.fx, j, y, ny, a.kxp);
-            pack_pairs(v, A, B, wj, j);
+            load_pairs(A, B, src[f], j, y, ny, a.kxp);
+            pack_pairs(v[f], A, B, wj, j);
         }
-        FFTi::run(v, j, 0, b0, b1, a.twx, 2, sync);
-#pragma unroll
-        for (int r = 0; r < R; r++) zx[r] = v[r];
-        {
-            cpx<T> A[R], B[R];
-            load_pairs(A, B, a.fa, j, y, ny, a.kxp);
-            pack_pairs(v, A, B, wj, j);
-        }
-        FFTi::run(v, j, 0, b0, b1, a.twx, 2, sync);
+        FFTi::template run_multi<3>(v, j, 0, b0, b1, a.twx, 2, sync);
 
-        // ---- real-space products; z[r] holds x = 2n (real part) and 2n + 1
-        // (imaginary part), n = j + r * TPC.  P overwrites zx, Q overwrites zy.
+        // ---- real-space products; v[f][r] holds x = 2n (real part) and
+        // 2n + 1 (imaginary part), n = j + r * TPC.  P replaces uy, Q replaces ux.
         T se = 0, sx = 0, sy = 0;
         const T lam = a.lam_s, bet = a.beta_s;
 #pragma unroll
         for (int r = 0; r < R; r++) {
-            T ux0 = zx[r].x, uy0 = zy[r].x, w0 = v[r].x;
-            T ux1 = zx[r].y, uy1 = zy[r].y, w1 = v[r].y;
+            T ux0 = v[1][r].x, uy0 = v[0][r].x, w0 = v[2][r].x;
+            T ux1 = v[1][r].y, uy1 = v[0][r].y, w1 = v[2][r].y;
             T s0 = ux0 * ux0 + uy0 * uy0, s1 = ux1 * ux1 + uy1 * uy1;
             se += s0 + s1;
             sx += s0 * ux0 + s1 * ux1;
             sy += s0 * uy0 + s1 * uy1;
-            zx[r] = mk(lam * w0 * ux0 + bet * s0 * uy0, lam * w1 * ux1 + bet * s1 * uy1);
-            zy[r] = mk(lam * w0 * uy0 - bet * s0 * ux0, lam * w1 * uy1 - bet * s1 * ux1);
+            v[0][r] = mk(lam * w0 * ux0 + bet * s0 * uy0, lam * w1 * ux1 + bet * s1 * uy1);
+            v[1][r] = mk(lam * w0 * uy0 - bet * s0 * ux0, lam * w1 * uy1 - bet * s1 * ux1);
         }
 
         // ---- row sums of |u|^2, |u|^2 ux, |u|^2 uy in double over the row
         {
             double t0 = se, t1 = sx, t2 = sy;
-            row_sum3(t0, t1, t2, j, reinterpret_cast<double *>(b0.d), sync);
+            row_sum3(t0, t1, t2, j, reinterpret_cast<double *>(b0[2].d), sync);
             if (active && j == 0) {
                 a.rowp[(size_t)y * 3 + 0] = t0;
                 a.rowp[(size_t)y * 3 + 1] = t1;
@@ -381,27 +368,32 @@ struct RowPass {
             }
         }
 
-        // ---- R2C along x of P and Q
-        // The pairing exchange uses the buffer the transform's last pass did not read.
-        const Buf &pb = (FFTf::NEXCH & 1) ? b1 : b0;
+        // ---- R2C along x of P and Q in lockstep; the pairing exchange of each
+        // uses the buffer its transform's last pass did not read
+        cpx<T>(&pq)[2][R] = *reinterpret_cast<cpx<T>(*)[2][R]>(&v[0]);
+        const Buf pb0[2] = {b0[0], b0[1]};
+        const Buf pb1[2] = {b1[0], b1[1]};
+        FFTf::template run_multi<2>(pq, j, 0, pb0, pb1, a.twx, 2, sync);
+        if constexpr (FFTf::NEXCH == 0) sync();
 #pragma unroll
         for (int f = 0; f < 2; f++) {
+            const Buf &pb = (FFTf::NEXCH & 1) ? pb1[f] : pb0[f];
 #pragma unroll
-            for (int r = 0; r < R; r++) v[r] = f == 0 ? zx[r] : zy[r];
-            FFTf::run(v, j, 0, b0, b1, a.twx, 2, sync);
-            if constexpr (FFTf::NEXCH == 0) sync();
+            for (int r = 0; r < R; r++) pb.put(j + r * TPC, 0, pq[f][r]);
+        }
+        sync();
+        const int kend = a.ntp * Tile<T>::W;   // the column pass reads kx < kend
 #pragma unroll
-            for (int r = 0; r < R; r++) pb.put(j + r * TPC, 0, v[r]);
-            sync();
+        for (int f = 0; f < 2; f++) {
+            const Buf &pb = (FFTf::NEXCH & 1) ? pb1[f] : pb0[f];
             cpx<T> *dst = f == 0 ? a.P : a.Q;
-            const int kend = a.ntp * Tile<T>::W;   // the column pass reads kx < kend
             static_for<0, R>([&](auto rc) {
                 constexpr int r = decltype(rc)::value;
                 const int k = j + r * TPC;
-                if (active && k < kend) dst[tidx<T>(k, y, ny)] = unpack_r<r>(v[r], pb.get((M - k) & (M - 1), 0), wj);
+                if (active && k < kend) dst[tidx<T>(k, y, ny)] = unpack_r<r>(pq[f][r], pb.get((M - k) & (M - 1), 0), wj);
             });
             if (active && j == 0 && M < kend) {   // kx = M: E(0) - O(0)
-                dst[tidx<T>(M, y, ny)] = unpack(v[0], v[0], mk<T>(-1, 0));
+                dst[tidx<T>(M, y, ny)] = unpack(pq[f][0], pq[f][0], mk<T>(-1, 0));
             }
             for (int kx = M + 1 + j; active && kx < kend; kx += TPC) dst[tidx<T>(kx, y, ny)] = mk<T>(0, 0);
         }

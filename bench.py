@@ -65,7 +65,7 @@ def apply_preset(cfg, precision):
 
 # DRAM read + write bytes per launch of each pass for this workload, from the
 # ncu capture summarised in profiles/k_row_k_col_2048_fp32_full.md
-NCU_TRAFFIC = {"row": 25.430e6 + 0.341e6, "col": 25.508e6 + 0.572e6}
+NCU_TRAFFIC = {"row": 25.426e6 + 0.402e6, "col": 25.514e6 + 0.551e6}
 
 
 def peaks():

@@ -113,12 +113,12 @@ static am_status alloc_and_tables(am_handle *h)
     CK(h, cudaMalloc(&h->twy, ny * sizeof(cpx<T>)));
     CK(h, cudaMalloc(&h->kxt, h->nt * W * sizeof(T)));
     CK(h, cudaMalloc(&h->kyt, ny * sizeof(T)));
-    CK(h, cudaMalloc(&h->rowp, (size_t)ny * 3 * sizeof(double)));
-    CK(h, cudaMemsetAsync(h->rowp, 0, (size_t)ny * 3 * sizeof(double), h->stream));
+    CK(h, cudaMalloc(&h->rowp, side_bytes(ny)));
+    CK(h, cudaMemsetAsync(h->rowp, 0, side_bytes(ny), h->stream));
     CK(h, cudaMalloc(&h->energy, ECAP * sizeof(double)));
     CK(h, cudaMalloc(&h->sc, sizeof(Scalars)));
     h->bytes += nx * sizeof(cpx<T>) + ny * sizeof(cpx<T>) + h->nt * W * sizeof(T) + ny * sizeof(T) +
-                (size_t)ny * 3 * sizeof(double) + ECAP * sizeof(double) + sizeof(Scalars);
+                side_bytes(ny) + ECAP * sizeof(double) + sizeof(Scalars);
 
     HostTables<T> t;
     StepArgs<T> &a = args_of<T>(h);
@@ -139,7 +139,7 @@ static am_status alloc_and_tables(am_handle *h)
     a.twy = (const cpx<T> *)h->twy;
     a.kxt = (const T *)h->kxt;
     a.kyt = (const T *)h->kyt;
-    a.rowp = h->rowp;
+    set_side<T>(a, h->rowp, ny);
     a.sc = h->sc;
     a.energy = h->energy;
 

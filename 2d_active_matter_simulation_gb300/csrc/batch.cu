@@ -171,7 +171,7 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
         cudaMalloc(&b->twy, b->ny * sizeof(cpx<float>)) != cudaSuccess ||
         cudaMalloc(&b->kxt, t.kx.size() * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&b->kyt, t.ky.size() * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&b->rowp, B * b->ny * 3 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&b->rowp, B * side_bytes(b->ny)) != cudaSuccess ||
         cudaMalloc(&b->energy, B * ECAP_B * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&b->sc, B * sizeof(Scalars)) != cudaSuccess ||
         cudaMalloc(&b->dargs, B * sizeof(StepArgs<float>)) != cudaSuccess)
@@ -180,7 +180,7 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
         cudaMemcpyAsync(b->twy, t.twy.data(), b->ny * sizeof(cpx<float>), cudaMemcpyHostToDevice, b->stream) ||
         cudaMemcpyAsync(b->kxt, t.kx.data(), t.kx.size() * sizeof(float), cudaMemcpyHostToDevice, b->stream) ||
         cudaMemcpyAsync(b->kyt, t.ky.data(), t.ky.size() * sizeof(float), cudaMemcpyHostToDevice, b->stream) ||
-        cudaMemsetAsync(b->rowp, 0, B * b->ny * 3 * sizeof(double), b->stream) ||
+        cudaMemsetAsync(b->rowp, 0, B * side_bytes(b->ny), b->stream) ||
         cudaStreamSynchronize(b->stream))
         return fail(AM_ERR_CUDA);
     for (int i = 0; i < nmembers; i++) {
@@ -197,7 +197,7 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
         a.twy = b->twy;
         a.kxt = b->kxt;
         a.kyt = b->kyt;
-        a.rowp = b->rowp + (size_t)i * b->ny * 3;
+        set_side<float>(a, reinterpret_cast<unsigned char *>(b->rowp) + i * side_bytes(b->ny), b->ny);
         a.sc = b->sc + i;
         a.energy = b->energy + (size_t)i * ECAP_B;
     }

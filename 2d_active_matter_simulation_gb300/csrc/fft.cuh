@@ -380,8 +380,9 @@ struct BlockFFT {
     // buffers.  The twiddles of a pass are formed once for all NF transforms
     // and one barrier per exchange serves all of them, and the NF independent
     // DFTs per thread give the scheduler more work between shared-memory
-    // accesses.
-    template <int NF, class Buf, class Sync>
+    // accesses.  SINGLE = 1: b1 is ignored and each transform reuses b0[f] for
+    // every exchange (one more barrier per exchange, half the shared memory).
+    template <int NF, int SINGLE = 0, class Buf, class Sync>
     static AF_HD void run_multi(cpx<T> (&v)[NF][R], int j, int c, const Buf (&b0)[NF], const Buf (&b1)[NF],
                                 const cpx<T> *tw, int TWS, Sync &&sync)
     {
@@ -405,10 +406,10 @@ struct BlockFFT {
             sync();
             e = 1;
         }
-        pass_multi<0, LOGR1 == 0, NF>(v, j, c, b0, b1, tw, TWS, sync, e);
+        pass_multi<0, LOGR1 == 0, NF, SINGLE>(v, j, c, b0, b1, tw, TWS, sync, e);
     }
 
-    template <int P, bool FROM_REGS, int NF, class Buf, class Sync>
+    template <int P, bool FROM_REGS, int NF, int SINGLE, class Buf, class Sync>
     static AF_HD void pass_multi(cpx<T> (&v)[NF][R], int j, int c, const Buf (&b0)[NF], const Buf (&b1)[NF],
                                  const cpx<T> *tw, int TWS, Sync &&sync, int e)
     {
@@ -417,7 +418,7 @@ struct BlockFFT {
             if constexpr (!FROM_REGS) {
 #pragma unroll
                 for (int f = 0; f < NF; f++) {
-                    const Buf &b = ((e & 1) == 1) ? b0[f] : b1[f];   // written by exchange e-1
+                    const Buf &b = (SINGLE || (e & 1) == 1) ? b0[f] : b1[f];   // written by exchange e-1
 #pragma unroll
                     for (int r = 0; r < R; r++) v[f][r] = b.d[b.template at<TPC>(j, r, c)];
                 }
@@ -437,14 +438,15 @@ struct BlockFFT {
             if constexpr (P < NPASS - 1) {
                 const int k = j & (NS - 1);
                 const int base = (j - k) * R + k;
+                if (SINGLE && e > 0) sync();   // one buffer: earlier reads must finish
 #pragma unroll
                 for (int f = 0; f < NF; f++) {
-                    const Buf &b = ((e & 1) == 0) ? b0[f] : b1[f];
+                    const Buf &b = (SINGLE || (e & 1) == 0) ? b0[f] : b1[f];
 #pragma unroll
                     for (int r = 0; r < R; r++) b.d[b.template at<NS>(base, r, c)] = v[f][r];
                 }
                 sync();
-                pass_multi<P + 1, false, NF>(v, j, c, b0, b1, tw, TWS, sync, e + 1);
+                pass_multi<P + 1, false, NF, SINGLE>(v, j, c, b0, b1, tw, TWS, sync, e + 1);
             }
         }
     }

@@ -30,6 +30,18 @@ struct HostTables {
 };
 
 // Fill the tables and every scalar field of `a` (pointers are left alone).
+// dt factors of the mean-flow stage updates, in double from dt as T: the same
+// values the column pass would get from its own divisions.
+template <typename T>
+void set_mean_flow_coeffs(StepArgs<T> &a)
+{
+    const double dd = (double)a.dt;
+    a.mf_d2 = dd / 2;
+    a.mf_d6 = dd / 6;
+    a.mf_d6l = dd / 6 * a.lin_v;
+    a.mf_d3l2 = dd / 3 * a.lin2_v;
+}
+
 template <typename T>
 void host_setup(const am_params &p, HostTables<T> &t, StepArgs<T> &a, int ecap)
 {
@@ -83,6 +95,7 @@ void host_setup(const am_params &p, HostTables<T> &t, StepArgs<T> &a, int ecap)
     const double L0 = p.form == AM_FORM_REFERENCE ? -(1.0 + p.alpha) : -p.alpha;
     a.lin_v = std::exp(L0 * p.dt);
     a.lin2_v = std::exp(L0 * p.dt / 2);
+    set_mean_flow_coeffs<T>(a);
     a.inv_2n3 = 1.0 / (2.0 * nd * nd * nd);
     a.mode = 0;
 }
@@ -93,6 +106,17 @@ void host_setup(const am_params &p, HostTables<T> &t, StepArgs<T> &a, int ecap)
 // there.  The stage fields then carry no data for kx > Nx/4: the column pass
 // skips those tiles and the row pass neither loads nor stores them.  The results
 // are those of the full transforms (the skipped entries are exact zeros).
+// Per-run side buffer: the row sums (3 * Ny values) followed by the two
+// halves of the kx = 0 column's w_new (2 * Ny complex), sized for double so
+// one layout serves both precisions.
+inline size_t side_bytes(int ny) { return (size_t)ny * (3 * sizeof(double) + 2 * 2 * sizeof(double)); }
+template <typename T>
+void set_side(StepArgs<T> &a, void *base, int ny)
+{
+    a.rowp = reinterpret_cast<T *>(base);
+    a.hcol = reinterpret_cast<cpx<T> *>(static_cast<unsigned char *>(base) + (size_t)ny * 3 * sizeof(double));
+}
+
 template <typename T>
 void set_pruning(StepArgs<T> &a, bool on)
 {

@@ -121,7 +121,7 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
     size_t o_ky = off;
     off += align256((size_t)ny * sizeof(T));
     size_t o_rowp = off;
-    off += align256((size_t)ny * 3 * sizeof(double));
+    off += align256(side_bytes(ny));
     size_t o_sc = off;
     off += align256(sizeof(Scalars));
     size_t o_ring = off;
@@ -152,7 +152,7 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
     a.twy = reinterpret_cast<const cpx<T> *>(base + o_twy);
     a.kxt = reinterpret_cast<const T *>(base + o_kx);
     a.kyt = reinterpret_cast<const T *>(base + o_ky);
-    a.rowp = reinterpret_cast<double *>(base + o_rowp);
+    set_side<T>(a, base + o_rowp, ny);
     a.sc = reinterpret_cast<Scalars *>(base + o_sc);
     a.energy = energy ? energy : reinterpret_cast<double *>(base + o_ring);
     a.ecap = energy ? (nsteps > 0 ? nsteps : 1) : 16;
@@ -173,6 +173,7 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
     const double L0 = p.form == AM_FORM_REFERENCE ? -(1.0 + p.alpha) : -p.alpha;
     a.lin_v = std::exp(L0 * p.dt);
     a.lin2_v = std::exp(L0 * p.dt / 2);
+    set_mean_flow_coeffs<T>(a);
     a.inv_2n3 = 1.0 / (2.0 * nd * nd * nd);
 
     const KernelTable<T> &K = table<T>();

@@ -40,6 +40,7 @@ struct Scalars {
     int status;                            // reserved device status word (0 = ok)
     int pad_;
 };
+static_assert(sizeof(Scalars) == 64, "the column pass copies Scalars as four 16-byte pieces");
 
 template <typename T>
 struct StepArgs {
@@ -48,13 +49,15 @@ struct StepArgs {
                                     // number of column tiles the passes touch (pruned
                                     // transforms: kxp = Nx/4 under the 1/2 rule)
     cpx<T> *u0, *acc;               // spectral state (kx, ky): w_old / w_new
+    cpx<T> *hcol;                   // w_new of the kx = 0 column, two halves of Ny
+                                    // (stages alternate: one is read, the other written)
     cpx<T> *fa, *fx, *fy;           // stage input a, ux, uy in (kx, y)
     cpx<T> *P, *Q;                  // products in (kx, y)
     const cpx<T> *twx;              // exp(-2 pi i m / Nx), m < Nx
     const cpx<T> *twy;              // exp(-2 pi i m / Ny), m < Ny
     const T *kxt;                   // kx wavenumbers, nt * W entries (0 past Nx/2)
     const T *kyt;                   // ky wavenumbers in FFT order, Ny entries
-    double *rowp;                   // per-row sums [Ny][3]: |u|^2, |u|^2 ux, |u|^2 uy
+    T *rowp;                        // per-row sums [3][Ny]: |u|^2, |u|^2 ux, |u|^2 uy
     Scalars *sc;
     double *energy;                 // energy per step, ring of ecap entries
     int ecap;
@@ -65,6 +68,7 @@ struct StepArgs {
     int dealias;                    // 0: reference (int32 radius), 1: 1/2 rule, 2: none
     int rsq;                        // reference mask radius^2 after 32-bit wrap
     double lin_v, lin2_v;           // mean-flow integrating factors
+    double mf_d2, mf_d6, mf_d6l, mf_d3l2;   // dt/2, dt/6, dt/6*lin_v, dt/3*lin2_v (dt as T, in double)
     double inv_2n3;                 // 1 / (2 N^3)
     int mode;                       // column pass: 0 = start from u0, 1..4 = RK stage
 };
@@ -257,11 +261,14 @@ struct RowPass {
         }
     }
 
-    // Sum (t0, t1, t2) over the TPC threads of a row; the result is valid in
-    // thread j = 0.  GPU: warp shuffles, then one shared-memory step across the
-    // row's warps.  Elsewhere: a shared-memory tree.
+    // Sum (t0, t1, t2) over the TPC threads of a row in T; the result is valid
+    // in thread j = 0.  GPU: warp shuffles, then one shared-memory step across
+    // the row's warps.  Elsewhere: a shared-memory tree.  (FP32 sums are at
+    // least as accurate as the reference's own: it sums the energy sequentially
+    // in float, ActFlow_V3-2.cu:1118-1124, and takes the mean-flow sums from the
+    // k = 0 term of a float FFT.)
     template <class Sync>
-    static AF_HD void row_sum3(double &t0, double &t1, double &t2, int j, double *scratch, Sync &&sync)
+    static AF_HD void row_sum3(T &t0, T &t1, T &t2, int j, T *scratch, Sync &&sync)
     {
 #ifdef __CUDA_ARCH__
         if constexpr (TPC >= 32) {
@@ -357,14 +364,14 @@ struct RowPass {
             v[1][r] = mk(lam * w0 * uy0 - bet * s0 * ux0, lam * w1 * uy1 - bet * s1 * ux1);
         }
 
-        // ---- row sums of |u|^2, |u|^2 ux, |u|^2 uy in double over the row
+        // ---- row sums of |u|^2, |u|^2 ux, |u|^2 uy over the row
         {
-            double t0 = se, t1 = sx, t2 = sy;
-            row_sum3(t0, t1, t2, j, reinterpret_cast<double *>(b0[2].d), sync);
+            T t0 = se, t1 = sx, t2 = sy;
+            row_sum3(t0, t1, t2, j, reinterpret_cast<T *>(b0[2].d), sync);
             if (active && j == 0) {
-                a.rowp[(size_t)y * 3 + 0] = t0;
-                a.rowp[(size_t)y * 3 + 1] = t1;
-                a.rowp[(size_t)y * 3 + 2] = t2;
+                a.rowp[y] = t0;
+                a.rowp[ny + y] = t1;
+                a.rowp[2 * ny + y] = t2;
             }
         }
 
@@ -403,6 +410,98 @@ struct RowPass {
 template <typename T, int LOGNX>
 using RowKernel = RowPass<T, LOGNX>;
 
+// ------------------------------------------------- sums over the row sums
+// Compensated ("float-float") accumulation for the FP32 path: hi + lo carries
+// about 44 significant bits, so the sum over all rows is as good as a double
+// sum while it stays on the FP32 pipes (FP64 throughput on this GPU is a small
+// fraction of FP32).  Two-sum after Knuth, TAOCP vol. 2, 4.2.2, theorem B.
+// The order of summation is fixed, so results are reproducible bit for bit.
+template <typename T>
+struct RowAcc {   // FP64 path: plain double
+    double v = 0;
+    AF_HD void add(T x) { v += (double)x; }
+    AF_HD void add(const RowAcc &o) { v += o.v; }
+    AF_HD double value() const { return v; }
+#ifdef __CUDA_ARCH__
+    __device__ void add_xor(int o) { v += __shfl_xor_sync(0xffffffffu, v, o); }
+#endif
+};
+template <>
+struct RowAcc<float> {
+    float hi = 0, lo = 0;
+    AF_HD void add2(float bh, float bl)
+    {
+        const float s = hi + bh;
+        const float bb = s - hi;
+        float e = (hi - (s - bb)) + (bh - bb);
+        e += lo + bl;
+        hi = s + e;
+        lo = e - (hi - s);
+    }
+    AF_HD void add(float x) { add2(x, 0.f); }
+    AF_HD void add(const RowAcc &o) { add2(o.hi, o.lo); }
+    AF_HD double value() const { return (double)hi + (double)lo; }
+#ifdef __CUDA_ARCH__
+    __device__ void add_xor(int o)
+    {
+        const float h = __shfl_xor_sync(0xffffffffu, hi, o), l = __shfl_xor_sync(0xffffffffu, lo, o);
+        add2(h, l);
+    }
+#endif
+};
+
+// 16-byte global -> shared copy that completes asynchronously (the thread
+// that issued it waits with cp_async_wait_all before reading the data).
+AF_HD void cp_async16(void *dst_smem, const void *src)
+{
+#ifdef __CUDA_ARCH__
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+#else
+    for (int i = 0; i < 16; i++) static_cast<unsigned char *>(dst_smem)[i] = static_cast<const unsigned char *>(src)[i];
+#endif
+}
+AF_HD void cp_async8(void *dst_smem, const void *src)
+{
+#ifdef __CUDA_ARCH__
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+#else
+    for (int i = 0; i < 8; i++) static_cast<unsigned char *>(dst_smem)[i] = static_cast<const unsigned char *>(src)[i];
+#endif
+}
+// Named barrier 1 (barrier 0 is __syncthreads): bar_arrive signals without
+// waiting, bar_wait waits until `n` threads have arrived or waited; prior
+// shared-memory writes of the arriving threads are visible after the wait.
+AF_HD void bar_arrive1(int n)
+{
+#ifdef __CUDA_ARCH__
+    asm volatile("bar.arrive 1, %0;\n" ::"r"(n) : "memory");
+#else
+    (void)n;
+#endif
+}
+AF_HD void bar_wait1(int n)
+{
+#ifdef __CUDA_ARCH__
+    asm volatile("bar.sync 1, %0;\n" ::"r"(n) : "memory");
+#else
+    (void)n;
+#endif
+}
+AF_HD void cp_async_commit()
+{
+#ifdef __CUDA_ARCH__
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+#endif
+}
+AF_HD void cp_async_wait_all()
+{
+#ifdef __CUDA_ARCH__
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+#endif
+}
+
 // --------------------------------------------------------------- column pass
 // One tile of W adjacent kx columns per group of W * TPC threads (lane c =
 // column inside the tile, j = thread of that column's transform), so every
@@ -422,8 +521,25 @@ struct ColPass {
     static constexpr int THREADS = TILES * W * TPC;
     using Buf = XBuf<T, W, 0>;
     static constexpr int BUFS = (Buf::slots(L) + 7) / 8 * 8;
+    // Shared memory: the exchange buffers; then what CTA 0 fetches at kernel
+    // start in stages 1-4 so that its extra serial work (the mean flow, the
+    // energy, the Hermitian repair) runs from shared memory: the Scalars, the
+    // source of the kx = 0 column's mirror values, the row sums; then one
+    // partial sum per warp.  The fetches are made only where they fit.
+    static constexpr size_t XB = (size_t)TILES * BUFS * sizeof(cpx<T>);
+    static constexpr size_t SCB = sizeof(Scalars);
+    static constexpr size_t MIB = (size_t)L * sizeof(cpx<T>);
+    static constexpr size_t PFB = (size_t)3 * L * sizeof(T);
+    static constexpr int NW = THREADS / 32;
+    static constexpr size_t WPB = (size_t)3 * NW * sizeof(RowAcc<T>);
+    static constexpr size_t LIM = (size_t)227 * 1024;
+    static constexpr bool PM = XB + SCB + MIB + WPB <= LIM;              // Scalars + mirror column
+    static constexpr bool PF = PM && XB + SCB + MIB + PFB + WPB <= LIM;  // + row sums
+    static constexpr size_t O_SC = XB, O_MI = XB + SCB, O_PF = O_MI + (PM ? MIB : 0);
+    static constexpr size_t O_WP = O_PF + (PF ? PFB : 0);
+    static constexpr int CE = 16 / (int)sizeof(T);                     // row sums per 16-byte copy
 
-    static constexpr size_t smem_bytes() { return (size_t)TILES * BUFS * sizeof(cpx<T>) + 8 * sizeof(double); }
+    static constexpr size_t smem_bytes() { return O_WP + WPB; }
 
     template <class Sync>
     static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync)
@@ -437,12 +553,46 @@ struct ColPass {
         const bool col = active && kx <= a.kxp;   // a column that carries data
         const int ny = a.ny, nx = a.nx;
         Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)tl * BUFS};
-        double *red = reinterpret_cast<double *>(smem);   // owner-CTA scratch, aliases the buffers
-        double *bc = reinterpret_cast<double *>(smem + (size_t)TILES * BUFS * sizeof(cpx<T>));
+        const Scalars *ssm = reinterpret_cast<const Scalars *>(smem + O_SC);   // owner copies
+        cpx<T> *mir = reinterpret_cast<cpx<T> *>(smem + O_MI);
+        T *rsm = reinterpret_cast<T *>(smem + O_PF);
+        RowAcc<T> *wp = reinterpret_cast<RowAcc<T> *>(smem + O_WP);   // warp partials
         const bool owner = bid == 0;   // this CTA holds column kx = 0
         const T kxv = active ? a.kxt[kx] : (T)0;
         const size_t cbase = active ? (size_t)tile * ny * W + c : 0;
         const T dt = a.dt;
+        // The kx = 0 column keeps w_new in a.hcol: stage 1 writes half 0,
+        // stage 2 reads 0 and writes 1, stage 3 reads 1 and writes 0, stage 4
+        // reads 0.  So the Hermitian repair can read the mirror values
+        // w_new(-ky) while this stage writes its results, without a barrier.
+        const cpx<T> *hin = a.hcol + (size_t)(MODE & 1) * ny;
+        cpx<T> *hout = a.hcol + (size_t)((MODE + 1) & 1) * ny;
+
+        // The owner fetches its extra inputs now.  The row sums are summed by
+        // the threads that copied them; the Scalars are read by thread 0, which
+        // copied them; the mirror column is read by other threads after the
+        // barrier at the start of the second forward transform.
+        if constexpr (MODE != 0 && PM) {
+            if (owner) {
+                if (tid < 4) cp_async16(smem + O_SC + 16 * tid, reinterpret_cast<const unsigned char *>(a.sc) + 16 * tid);
+                if constexpr (MODE == 1) {   // w_old of the kx = 0 column (tile 0, lane 0)
+                    for (int y = tid; y < ny; y += THREADS) {
+                        if constexpr (sizeof(cpx<T>) == 8) cp_async8(mir + y, a.u0 + (size_t)y * W);
+                        else cp_async16(mir + y, a.u0 + (size_t)y * W);
+                    }
+                } else {
+                    constexpr int CC = 16 / (int)sizeof(cpx<T>);
+                    for (int q = tid; q < ny / CC; q += THREADS) cp_async16(mir + q * CC, hin + q * CC);
+                }
+                if constexpr (PF) {
+#pragma unroll
+                    for (int k = 0; k < 3; k++)
+                        for (int q = tid; q < ny / CE; q += THREADS)
+                            cp_async16(rsm + (size_t)k * ny + q * CE, a.rowp + (size_t)k * ny + q * CE);
+                }
+                cp_async_commit();
+            }
+        }
 
         // ---- forward FFT along y of P and Q, N = i (-kx P^ - ky Q^) * mask
         cpx<T> nl[R];
@@ -455,6 +605,14 @@ struct ColPass {
             for (int r = 0; r < R; r++) ph[r] = v[r];
 #pragma unroll
             for (int r = 0; r < R; r++) v[r] = active ? a.Q[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
+            if constexpr (PM) {
+                // the owner's copies are complete; the barrier that starts the
+                // next transform makes them visible to the whole CTA
+                if (owner) {
+                    cp_async_wait_all();
+                    if constexpr (FFTf::NEXCH == 0) sync();
+                }
+            }
             FFTf::run(v, j, c, buf, a.twy, 1, sync);
             const ColMask cm(a.dealias, a.rsq, nx, ny, kx);
 #pragma unroll
@@ -468,126 +626,118 @@ struct ColPass {
             }
         }
 
-        // ---- mean flow and energy: reduce the row sums (CTA holding kx = 0)
-        if (owner) {
-            double se = 0, sx = 0, sy = 0;
-            if constexpr (MODE != 0) {
-                for (int y = tid; y < ny; y += THREADS) {
-                    se += a.rowp[(size_t)y * 3 + 0];
-                    sx += a.rowp[(size_t)y * 3 + 1];
-                    sy += a.rowp[(size_t)y * 3 + 2];
-                }
-            }
-            sync();
-            red[tid] = se;
-            red[THREADS + tid] = sx;
-            red[2 * THREADS + tid] = sy;
-            sync();
-            for (int s = THREADS / 2; s > 0; s >>= 1) {
-                if (tid < s) {
-                    red[tid] += red[tid + s];
-                    red[THREADS + tid] += red[THREADS + tid + s];
-                    red[2 * THREADS + tid] += red[2 * THREADS + tid + s];
-                }
-                sync();
-            }
-            if (tid == 0) {
-                Scalars *s = a.sc;
-                // Mean-flow right-hand side -beta' Re F[|u|^2 u](0)
-                // (ActFlow_V3-2.cu:1086-1087) and its stage updates
-                // (ActFlow_V3-2.cu:729-732, 756-759, 778-781, 799-802, 820-821).
-                const double n0 = -a.beta_sd * red[THREADS], n1 = -a.beta_sd * red[2 * THREADS];
-                const double dd = (double)dt;
-                if constexpr (MODE == 0) {
-                    for (int d = 0; d < 2; d++) s->m_old[d] = s->m_appr[d] = s->m_new[d];
-                } else if constexpr (MODE == 1) {
-                    a.energy[s->step % a.ecap] = red[0] * a.inv_2n3;
-                    s->m_new[0] += dd / 6 * a.lin_v * n0;
-                    s->m_new[1] += dd / 6 * a.lin_v * n1;
-                    s->m_appr[0] = a.lin2_v * (s->m_old[0] + dd / 2 * n0);
-                    s->m_appr[1] = a.lin2_v * (s->m_old[1] + dd / 2 * n1);
-                } else if constexpr (MODE == 2) {
-                    s->m_new[0] += dd / 3 * a.lin2_v * n0;
-                    s->m_new[1] += dd / 3 * a.lin2_v * n1;
-                    s->m_appr[0] = a.lin2_v * (s->m_old[0] + dd / 2 * n0);
-                    s->m_appr[1] = a.lin2_v * (s->m_old[1] + dd / 2 * n1);
-                } else if constexpr (MODE == 3) {
-                    s->m_new[0] += dd / 3 * a.lin2_v * n0;
-                    s->m_new[1] += dd / 3 * a.lin2_v * n1;
-                    s->m_appr[0] = a.lin_v * (s->m_old[0] + dd * n0);
-                    s->m_appr[1] = a.lin_v * (s->m_old[1] + dd * n1);
-                } else {
-                    s->m_new[0] += dd / 6 * n0;
-                    s->m_new[1] += dd / 6 * n1;
-                    for (int d = 0; d < 2; d++) s->m_old[d] = s->m_appr[d] = s->m_new[d];
-                }
-                bc[0] = s->m_appr[0];
-                bc[1] = s->m_appr[1];
-            }
-            sync();
-        }
-
         // ---- RK stage combination (integrate_func_0..4, ActFlow_V3-2.cu:940-1018)
         // with the Hermitian repair of the accumulator's kx = 0 column before the
-        // addition (reality_func, ActFlow_V3-2.cu:1228-1243).
-        cpx<T> av[R];
+        // addition (reality_func, ActFlow_V3-2.cu:1228-1243).  Its loads are
+        // issued before the owner's mean-flow work so that their latency
+        // overlaps it.
+        cpx<T> av[R], accv[R];
+        const bool c0 = owner && tl == 0 && c == 0;   // the kx = 0 column
         if constexpr (MODE == 0) {
 #pragma unroll
             for (int r = 0; r < R; r++) av[r] = active ? a.u0[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
         } else {
-            cpx<T> accv[R];
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 size_t g = cbase + (size_t)(j + r * TPC) * W;
                 if constexpr (MODE == 1) {
                     av[r] = active ? a.u0[g] : mk<T>(0, 0);   // w_old
-                    T e2 = lin_at(a, kxv, j + r * TPC, dt / 2);
-                    accv[r] = scale(av[r], e2 * e2);          // w_new = w_old * lin
                 } else {
-                    accv[r] = active ? a.acc[g] : mk<T>(0, 0);
+                    accv[r] = c0 ? hin[j + r * TPC] : active ? a.acc[g] : mk<T>(0, 0);
                     if constexpr (MODE != 4) av[r] = active ? a.u0[g] : mk<T>(0, 0);
                 }
             }
-            if (owner) {
-                sync();
-                if (tl == 0 && c == 0) {
+        }
+
+        // ---- mean flow and energy: reduce the row sums (CTA holding kx = 0)
+        T m0 = 0, m1 = 0;          // mean velocity for the k = 0 slot (thread 0 of the owner)
+        int sc_step = 0, sc_nan = 0;   // step counters (thread 0 of the owner)
+        if (owner) {
+            RowAcc<T> sum[3];
+            if constexpr (MODE != 0) {
 #pragma unroll
-                    for (int r = 0; r < R; r++) buf.put(j + r * TPC, 0, accv[r]);
-                }
-                sync();
-                if (tl == 0 && c == 0) {
+                for (int k = 0; k < 3; k++)
+                    for (int q = tid; q < ny / CE; q += THREADS) {
+                        const T *src = (PF ? rsm : a.rowp) + (size_t)k * ny + q * CE;
 #pragma unroll
-                    for (int r = 0; r < R; r++) {
-                        int iy = j + r * TPC;
-                        if (iy >= 1 && iy < ny / 2) {
-                            cpx<T> b = buf.get(ny - iy, 0);
-                            accv[r] = mk((T)0.5f * (accv[r].x + b.x), (T)0.5f * (accv[r].y - b.y));
-                        } else if (iy > ny / 2) {
-                            cpx<T> b = buf.get(ny - iy, 0);
-                            accv[r] = conj(mk((T)0.5f * (b.x + accv[r].x), (T)0.5f * (b.y - accv[r].y)));
-                        }
+                        for (int e = 0; e < CE; e++) sum[k].add(src[e]);
                     }
-                }
             }
+            block_sum3(sum, tid, wp, sync);
+            if (tid == 0) {
+                Scalars s = (MODE != 0 && PM) ? *ssm : *a.sc;
+                const double red[3] = {sum[0].value(), sum[1].value(), sum[2].value()};
+                // Mean-flow right-hand side -beta' Re F[|u|^2 u](0)
+                // (ActFlow_V3-2.cu:1086-1087) and its stage updates
+                // (ActFlow_V3-2.cu:729-732, 756-759, 778-781, 799-802, 820-821).
+                // (the dt factors come precomputed from the host: no FP64
+                // division on this serial path)
+                const double n0 = -a.beta_sd * red[1], n1 = -a.beta_sd * red[2];
+                const double dd = (double)dt;
+                if constexpr (MODE == 0) {
+                    for (int d = 0; d < 2; d++) s.m_old[d] = s.m_appr[d] = s.m_new[d];
+                } else if constexpr (MODE == 1) {
+                    a.energy[s.step % a.ecap] = red[0] * a.inv_2n3;
+                    s.m_new[0] += a.mf_d6l * n0;
+                    s.m_new[1] += a.mf_d6l * n1;
+                    s.m_appr[0] = a.lin2_v * (s.m_old[0] + a.mf_d2 * n0);
+                    s.m_appr[1] = a.lin2_v * (s.m_old[1] + a.mf_d2 * n1);
+                } else if constexpr (MODE == 2) {
+                    s.m_new[0] += a.mf_d3l2 * n0;
+                    s.m_new[1] += a.mf_d3l2 * n1;
+                    s.m_appr[0] = a.lin2_v * (s.m_old[0] + a.mf_d2 * n0);
+                    s.m_appr[1] = a.lin2_v * (s.m_old[1] + a.mf_d2 * n1);
+                } else if constexpr (MODE == 3) {
+                    s.m_new[0] += a.mf_d3l2 * n0;
+                    s.m_new[1] += a.mf_d3l2 * n1;
+                    s.m_appr[0] = a.lin_v * (s.m_old[0] + dd * n0);
+                    s.m_appr[1] = a.lin_v * (s.m_old[1] + dd * n1);
+                } else {
+                    s.m_new[0] += a.mf_d6 * n0;
+                    s.m_new[1] += a.mf_d6 * n1;
+                    for (int d = 0; d < 2; d++) s.m_old[d] = s.m_appr[d] = s.m_new[d];
+                }
+                Scalars *g = a.sc;
+                for (int d = 0; d < 2; d++) {
+                    g->m_old[d] = s.m_old[d];
+                    g->m_new[d] = s.m_new[d];
+                    g->m_appr[d] = s.m_appr[d];
+                }
+                m0 = (T)s.m_appr[0];
+                m1 = (T)s.m_appr[1];
+                sc_step = s.step;
+                sc_nan = s.nan_step;
+            }
+        }
+
+        if constexpr (MODE != 0) {
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 const int iy = j + r * TPC;
                 const size_t g = cbase + (size_t)iy * W;
                 const cpx<T> n = nl[r], o = av[r];
-                cpx<T> w = accv[r];
-                // exp(L dt) is formed as exp(L dt / 2)^2 (one exponential per value)
+                // exp(L dt / 2) at (kx, ky); exp(L dt) is formed as its square.
+                // ky(-iy) = -ky(iy) exactly, so the mirror shares this value.
+                const T e2 = MODE == 4 ? (T)0 : lin_at(a, kxv, iy, dt / 2);
+                cpx<T> w = MODE == 1 ? scale(o, e2 * e2) : accv[r];   // stage 1: w_new = w_old * lin
+                if (c0 && iy != 0 && iy != ny / 2) {
+                    // Hermitian repair with the mirror value w_new(-ky)
+                    const int my = ny - iy;
+                    cpx<T> b;
+                    if constexpr (MODE == 1) b = scale(PM ? mir[my] : a.u0[cbase + (size_t)my * W], e2 * e2);
+                    else b = PM ? mir[my] : hin[my];
+                    if (iy < ny / 2) w = mk((T)0.5f * (w.x + b.x), (T)0.5f * (w.y - b.y));
+                    else w = conj(mk((T)0.5f * (b.x + w.x), (T)0.5f * (b.y - w.y)));
+                }
                 if constexpr (MODE == 1) {
-                    T e2 = lin_at(a, kxv, iy, dt / 2);
                     T f = dt / 6 * (e2 * e2);
                     w = mk(w.x + f * n.x, w.y + f * n.y);
                     av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), e2);
                 } else if constexpr (MODE == 2) {
-                    T e2 = lin_at(a, kxv, iy, dt / 2);
                     T f = dt / 3 * e2;
                     w = mk(w.x + f * n.x, w.y + f * n.y);
                     av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), e2);
                 } else if constexpr (MODE == 3) {
-                    T e2 = lin_at(a, kxv, iy, dt / 2);
                     T f = dt / 3 * e2;
                     w = mk(w.x + f * n.x, w.y + f * n.y);
                     av[r] = scale(mk(o.x + dt * n.x, o.y + dt * n.y), e2 * e2);
@@ -597,15 +747,15 @@ struct ColPass {
                 }
                 if (active) {
                     if constexpr (MODE == 4) a.u0[g] = w;
+                    else if (c0) hout[iy] = w;
                     else a.acc[g] = w;
                 }
             }
             if constexpr (MODE == 4) {
                 if (owner && tid == 0) {
                     // NaN probe on Re w(0,0) (check_func, ActFlow_V3-2.cu:884-897).
-                    Scalars *s = a.sc;
-                    if (av[0].x != av[0].x && s->nan_step < 0) s->nan_step = s->step;
-                    s->step += 1;
+                    if (av[0].x != av[0].x && sc_nan < 0) a.sc->nan_step = sc_step;
+                    a.sc->step = sc_step + 1;
                 }
             }
         }
@@ -613,11 +763,6 @@ struct ColPass {
         // ---- Biot-Savart (nonl_subfunc_0, ActFlow_V3-2.cu:1176-1180) and the
         // mean velocity in the k = 0 slot (ActFlow_V3-2.cu:1053-1054), then the
         // inverse FFT along y of a, ux, uy.
-        T m0 = 0, m1 = 0;
-        if (owner) {
-            m0 = (T)bc[0];
-            m1 = (T)bc[1];
-        }
 #pragma unroll 1
         for (int f = 0; f < 3; f++) {
             cpx<T> v[R];
@@ -642,6 +787,62 @@ struct ColPass {
                 for (int r = 0; r < R; r++) dst[cbase + (size_t)(j + r * TPC) * W] = v[r];
             }
         }
+    }
+
+    // Sum the three accumulators over the CTA; the result is valid in thread 0.
+    // GPU: warp shuffles, one partial per warp in shared memory; warps 1.. go
+    // on after leaving their partial (named barrier, arrive only), warp 0 waits
+    // for them and combines the partials with shuffles.  Elsewhere: the
+    // partials from a per-warp loop, then thread 0 adds them in warp order.
+    template <class Sync>
+    static AF_HD void block_sum3(RowAcc<T> (&sum)[3], int tid, RowAcc<T> *wp, Sync &&sync)
+    {
+#ifdef __CUDA_ARCH__
+        static_assert(NW <= 32, "one partial per lane of warp 0");
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) sum[k].add_xor(o);
+        }
+        if ((tid & 31) == 0) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) wp[(tid >> 5) * 3 + k] = sum[k];
+        }
+        if (tid >= 32) {
+            bar_arrive1(THREADS);
+            return;
+        }
+        bar_wait1(THREADS);
+#pragma unroll
+        for (int k = 0; k < 3; k++) sum[k] = tid < NW ? wp[tid * 3 + k] : RowAcc<T>{};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) sum[k].add_xor(o);
+        }
+        (void)sync;
+#else
+        // host emulation: each warp's partial is gathered in lane order
+        for (int lane = 0; lane < 32; lane++) {
+            if ((tid & 31) == lane) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    if (lane == 0) wp[(tid >> 5) * 3 + k] = sum[k];
+                    else wp[(tid >> 5) * 3 + k].add(sum[k]);
+                }
+            }
+            sync();
+        }
+        if (tid == 0) {
+            RowAcc<T> t[3] = {wp[0], wp[1], wp[2]};
+            for (int w = 1; w < NW; w++) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) t[k].add(wp[w * 3 + k]);
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) sum[k] = t[k];
+        }
+#endif
     }
 
     // exp(L(k) h) at (kx, ky index iy): L = -(1 - k^2)^2 - alpha (lin_func,

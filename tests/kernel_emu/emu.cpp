@@ -49,11 +49,11 @@ struct Runner {
         const int W = Tile<T>::W, nx = p.nx, ny = p.ny;
         const size_t fsz = (size_t)t.nt * W * ny;
         std::vector<cpx<T>> u0(fsz), acc(fsz), fa(fsz), fx(fsz), fy(fsz), P(fsz), Q(fsz);
-        std::vector<double> rowp((size_t)ny * 3), en(1 << 16);
+        std::vector<double> rowp(side_bytes(ny) / sizeof(double)), en(1 << 16);
         Scalars sc{};
         a.u0 = u0.data(); a.acc = acc.data(); a.fa = fa.data(); a.fx = fx.data(); a.fy = fy.data();
         a.P = P.data(); a.Q = Q.data(); a.twx = t.twx.data(); a.twy = t.twy.data();
-        a.kxt = t.kx.data(); a.kyt = t.ky.data(); a.rowp = rowp.data(); a.sc = &sc; a.energy = en.data();
+        a.kxt = t.kx.data(); a.kyt = t.ky.data(); set_side<T>(a, rowp.data(), ny); a.sc = &sc; a.energy = en.data();
         // tile the input
         for (int y = 0; y < ny; y++)
             for (int k = 0; k < t.nxh; k++) {
@@ -152,6 +152,24 @@ int dispatch_x(int ly, const am_params &p, T *w, double *m, int n, double *e, co
     case 6: return dispatch_y<T, LX, 6>(p, w, m, n, e, real, fwd, mask);
     case 7: return dispatch_y<T, LX, 7>(p, w, m, n, e, real, fwd, mask);
     }
+    if constexpr (LX <= 4) {   // long columns with few of them: the column kernels at production lengths
+        switch (ly) {
+        case 9: return dispatch_y<T, LX, 9>(p, w, m, n, e, real, fwd, mask);
+        case 10: return dispatch_y<T, LX, 10>(p, w, m, n, e, real, fwd, mask);
+        case 11: return dispatch_y<T, LX, 11>(p, w, m, n, e, real, fwd, mask);
+        }
+    }
+    return -100;
+}
+
+// Long rows with few of them: the row kernels at production lengths.
+template <typename T, int LX>
+int dispatch_long_x(int ly, const am_params &p, T *w, double *m, int n, double *e, const T *real, int fwd, int mask)
+{
+    switch (ly) {
+    case 3: return dispatch_y<T, LX, 3>(p, w, m, n, e, real, fwd, mask);
+    case 4: return dispatch_y<T, LX, 4>(p, w, m, n, e, real, fwd, mask);
+    }
     return -100;
 }
 
@@ -167,6 +185,9 @@ int dispatch(const am_params &p, T *w, double *m, int n, double *e, const T *rea
     case 5: return dispatch_x<T, 5>(ly, p, w, m, n, e, real, fwd, mask);
     case 6: return dispatch_x<T, 6>(ly, p, w, m, n, e, real, fwd, mask);
     case 7: return dispatch_x<T, 7>(ly, p, w, m, n, e, real, fwd, mask);
+    case 9: return dispatch_long_x<T, 9>(ly, p, w, m, n, e, real, fwd, mask);
+    case 10: return dispatch_long_x<T, 10>(ly, p, w, m, n, e, real, fwd, mask);
+    case 11: return dispatch_long_x<T, 11>(ly, p, w, m, n, e, real, fwd, mask);
     }
     return -100;
 }
@@ -175,7 +196,8 @@ int dispatch(const am_params &p, T *w, double *m, int n, double *e, const T *rea
 
 extern "C" {
 // Advance (w_hat [ny][nx/2+1] complex of the precision, mean[2]) nsteps steps.
-// Returns the first NaN step or -1; -100 for an unsupported size (8..128).
+// Returns the first NaN step or -1; -100 for an unsupported size (8..128 each,
+// or one side 512..2048 with the other 8..16).
 int emu_run(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy)
 {
     if (p->precision == AM_FP64)

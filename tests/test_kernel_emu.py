@@ -102,3 +102,31 @@ def test_emulated_pruned_half_rule(am, orc, emu, n, prec):
     assert np.abs(e - eo).max() <= tol * np.abs(eo).max()
     mask = orc.mask(nx, ny, "half")
     assert np.abs(w[mask == 0]).max() == 0.0
+
+
+@pytest.mark.parametrize("n", [(2048, 16), (16, 2048)])
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("kind", ["full", "pruned"])
+def test_emulated_production_lengths(am, orc, emu, n, prec, kind):
+    """The row kernel at Nx = 2048 and the column kernel at Ny = 2048 (the
+    benchmark's transform lengths), with few rows or columns so that the
+    emulation stays quick.  A unit-variance white-noise field and dt = 1e-3
+    make the nonlinear term about 1e-3 of the result, so FP64 agreement to
+    1e-13 pins the nonlinear term to about 1e-10.  "pruned": the state is
+    zeroed outside the 1/2-rule ellipse, so the kernels carry kx <= Nx/4 only."""
+    nx, ny = n
+    w0 = np.fft.rfft2(np.random.default_rng(nx + 7 * ny).standard_normal((ny, nx)))
+    dealias = "half"
+    if kind == "pruned":
+        w0 = w0 * orc.mask(nx, ny, "half")
+    p = am.Params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, 0.0, 0.0, 0, am.DEALIAS[dealias], prec)
+    w, m, e = _emu_run(am, emu, p, w0, (3.0, 1.0), 3)
+    op = orc.make_params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, dealias=dealias)
+    wo, mo, eo = orc.run(op, w0, (3.0, 1.0), 3, "f64")
+    w_lin, _, _ = orc.run(orc.make_params(nx, ny, 10.0, 12.0, 1e-3, 0.0, -0.8, 0.0, dealias=dealias), w0,
+                          (3.0, 1.0), 3, "f64")
+    assert np.linalg.norm(wo - w_lin) / np.linalg.norm(wo) > 1e-4   # the nonlinear term matters
+    tol = 1e-13 if prec else 2e-6
+    assert np.linalg.norm(w - wo) / np.linalg.norm(wo) < tol
+    assert np.abs(m - mo).max() <= tol * np.abs(mo).max()
+    assert np.abs(e - eo).max() <= tol * np.abs(eo).max()

@@ -21,7 +21,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libactflow.so")
 CLI_PATH = os.path.join(HERE, "lib", "actflow")
 
-AM_OK, AM_ERR_ARG, AM_ERR_CUDA, AM_ERR_NAN, AM_ERR_IO, AM_ERR_SPEC, AM_ERR_OOM, AM_ERR_UNSUPPORTED = range(8)
+(AM_OK, AM_ERR_ARG, AM_ERR_CUDA, AM_ERR_NAN, AM_ERR_IO, AM_ERR_SPEC, AM_ERR_OOM, AM_ERR_UNSUPPORTED,
+ AM_ERR_TIMEOUT) = range(9)
+ORDER = {"arrival": 0, "shortest": 1}
 FP32, FP64 = 0, 1
 DEALIAS = {"reference": 0, "half": 1, "none": 2}
 FORM_REFERENCE, FORM_GENERAL = 0, 1
@@ -47,6 +49,32 @@ class Spec(ctypes.Structure):
         ("has_gamma", ctypes.c_int), ("precision", ctypes.c_int), ("dealias", ctypes.c_int),
         ("initial", ctypes.c_char * 256), ("directory", ctypes.c_char * 1024),
     ]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_longlong), ("max_active", ctypes.c_int),
+                ("chunk_steps", ctypes.c_int), ("order", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("params", Params), ("nsteps", ctypes.c_longlong), ("w_hat", ctypes.c_void_p),
+                ("mean", ctypes.c_double * 2), ("seed", ctypes.c_ulonglong), ("kmin", ctypes.c_double),
+                ("kmax", ctypes.c_double), ("rms", ctypes.c_double), ("want_state", ctypes.c_int),
+                ("want_energy", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+
+
+class JobResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_longlong), ("status", ctypes.c_int), ("t_submit", ctypes.c_double),
+                ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double), ("mean", ctypes.c_double * 2),
+                ("steps_done", ctypes.c_longlong), ("error", ctypes.c_char * 256)]
+
+
+class ServerInfo(ctypes.Structure):
+    _fields_ = [("elapsed_s", ctypes.c_double), ("jobs_submitted", ctypes.c_longlong),
+                ("jobs_done", ctypes.c_longlong), ("jobs_pending", ctypes.c_longlong),
+                ("jobs_active", ctypes.c_int), ("peak_active", ctypes.c_int),
+                ("grid_point_steps", ctypes.c_longlong), ("device_bytes_reserved", ctypes.c_longlong),
+                ("peak_device_bytes", ctypes.c_longlong)]
 
 
 class ActflowError(RuntimeError):
@@ -95,6 +123,22 @@ def _load():
         "am_batch_get_state": ([hp, ctypes.c_int, vp, dp], ctypes.c_int),
         "am_batch_step": ([hp, ctypes.c_int, dp, ip], ctypes.c_int),
         "am_batch_last_error": ([hp], ctypes.c_char_p),
+        "am_ragged_create": ([ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_longlong), ctypes.c_int,
+                              ctypes.POINTER(hp)], ctypes.c_int),
+        "am_ragged_destroy": ([hp], ctypes.c_int),
+        "am_ragged_set_state": ([hp, ctypes.c_int, vp, dp], ctypes.c_int),
+        "am_ragged_get_state": ([hp, ctypes.c_int, vp, dp], ctypes.c_int),
+        "am_ragged_run": ([hp, ctypes.POINTER(dp), ip, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+        "am_ragged_device_bytes": ([hp], ctypes.c_longlong),
+        "am_ragged_classes": ([hp], ctypes.c_int),
+        "am_ragged_last_error": ([hp], ctypes.c_char_p),
+        "am_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(hp)], ctypes.c_int),
+        "am_server_submit": ([hp, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+        "am_server_wait": ([hp, ctypes.c_longlong, ctypes.c_double, ctypes.POINTER(JobResult), vp, dp],
+                           ctypes.c_int),
+        "am_server_stats": ([hp, ctypes.POINTER(ServerInfo)], ctypes.c_int),
+        "am_server_destroy": ([hp], ctypes.c_int),
+        "am_footprint_bytes": ([ctypes.POINTER(Params)], ctypes.c_longlong),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -113,6 +157,10 @@ EXPORTED = [
     "am_last_error", "am_mask_value", "am_ic_bandlimited", "am_spec_read", "am_write_snapshot",
     "am_read_snapshot", "am_append_energy", "am_cli_main", "am_batch_create", "am_batch_destroy",
     "am_batch_set_state", "am_batch_get_state", "am_batch_step", "am_batch_last_error",
+    "am_ragged_create", "am_ragged_destroy", "am_ragged_set_state", "am_ragged_get_state", "am_ragged_run",
+    "am_ragged_device_bytes", "am_ragged_classes", "am_ragged_last_error",
+    "am_server_create", "am_server_submit", "am_server_wait", "am_server_stats", "am_server_destroy",
+    "am_footprint_bytes",
 ]
 
 
@@ -258,6 +306,126 @@ class Batch:
         st = lib.am_batch_step(self.h, nsteps, _dptr(e) if energy else None, ctypes.byref(nan_m))
         self._chk(st, "am_batch_step")
         return e[:nsteps]
+
+
+class Ragged:
+    """Simulations of different grids, parameters and step counts advanced together (am_ragged)."""
+
+    def __init__(self, params_list, nsteps):
+        n = len(params_list)
+        arr = (Params * n)(*params_list)
+        steps = (ctypes.c_longlong * n)(*[int(k) for k in nsteps])
+        self.shapes = [(p.ny, p.nx // 2 + 1) for p in params_list]
+        self.nsteps = [int(k) for k in nsteps]
+        self.n = n
+        self.h = ctypes.c_void_p()
+        _check(lib.am_ragged_create(arr, steps, n, ctypes.byref(self.h)), None, "am_ragged_create")
+
+    def _chk(self, st, what):
+        if st != AM_OK:
+            raise ActflowError(st, f"{what}: {status_string(st)} {lib.am_ragged_last_error(self.h).decode()}")
+
+    def close(self):
+        if self.h:
+            lib.am_ragged_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, run, w_hat, mean=(0.0, 0.0)):
+        w = np.ascontiguousarray(w_hat, dtype=np.complex64)
+        assert w.shape == self.shapes[run]
+        m = np.array(mean, dtype=np.float64)
+        self._chk(lib.am_ragged_set_state(self.h, run, w.ctypes.data, _dptr(m)), "am_ragged_set_state")
+
+    def get_state(self, run):
+        w = np.zeros(self.shapes[run], dtype=np.complex64)
+        m = np.zeros(2)
+        self._chk(lib.am_ragged_get_state(self.h, run, w.ctypes.data, _dptr(m)), "am_ragged_get_state")
+        return w, m
+
+    def run(self, energy=True):
+        """Advance every run to its step count; returns (energies per run or None, grid-point-steps)."""
+        es = [np.zeros(max(k, 1)) for k in self.nsteps] if energy else None
+        ptrs = (ctypes.POINTER(ctypes.c_double) * self.n)(*[_dptr(e) for e in es]) if energy else None
+        nan_r = ctypes.c_int(-1)
+        gps = ctypes.c_longlong(0)
+        self._chk(lib.am_ragged_run(self.h, ptrs, ctypes.byref(nan_r), ctypes.byref(gps)), "am_ragged_run")
+        return ([e[:k] for e, k in zip(es, self.nsteps)] if energy else None), gps.value
+
+    @property
+    def classes(self):
+        return lib.am_ragged_classes(self.h)
+
+    @property
+    def device_bytes(self):
+        return lib.am_ragged_device_bytes(self.h)
+
+
+class Server:
+    """Continuous-batching simulation server on one GPU (am_server)."""
+
+    def __init__(self, hbm_budget_bytes=0, max_active=0, chunk_steps=0, order="arrival"):
+        cfg = ServerConfig(int(hbm_budget_bytes), int(max_active), int(chunk_steps), ORDER[order])
+        self.h = ctypes.c_void_p()
+        _check(lib.am_server_create(ctypes.byref(cfg), ctypes.byref(self.h)), None, "am_server_create")
+        self._jobs = {}
+
+    def submit(self, params, nsteps, seed=0, kmin=1.0, kmax=8.0, rms=0.01, w_hat=None, mean=(0.0, 0.0),
+               want_state=True, want_energy=True):
+        j = Job()
+        j.params = params
+        j.nsteps = int(nsteps)
+        keep = None
+        if w_hat is not None:
+            keep = np.ascontiguousarray(w_hat, dtype=np.complex128 if params.precision == FP64 else np.complex64)
+            j.w_hat = keep.ctypes.data
+        j.mean[0], j.mean[1] = mean
+        j.seed, j.kmin, j.kmax, j.rms = int(seed), kmin, kmax, rms
+        j.want_state, j.want_energy = int(want_state), int(want_energy)
+        jid = ctypes.c_longlong(0)
+        _check(lib.am_server_submit(self.h, ctypes.byref(j), ctypes.byref(jid)), None, "am_server_submit")
+        self._jobs[jid.value] = (params.nx, params.ny, params.precision, int(nsteps), want_state, want_energy)
+        return jid.value
+
+    def wait(self, jid, timeout=-1.0):
+        """Result dict of request jid: status, times, mean, state (if kept), energy (if kept)."""
+        nx, ny, prec, nsteps, ws, we = self._jobs[jid]
+        w = np.zeros((ny, nx // 2 + 1), dtype=np.complex128 if prec == FP64 else np.complex64) if ws else None
+        e = np.zeros(max(nsteps, 1)) if we else None
+        r = JobResult()
+        st = lib.am_server_wait(self.h, jid, timeout, ctypes.byref(r), w.ctypes.data if ws else None,
+                                _dptr(e) if we else None)
+        if st == AM_ERR_TIMEOUT:
+            raise ActflowError(st, f"request {jid}: timed out")
+        del self._jobs[jid]
+        return {"id": r.id, "status": r.status, "error": r.error.decode(), "t_submit": r.t_submit,
+                "t_admit": r.t_admit, "t_done": r.t_done, "mean": np.array(r.mean[:]), "steps_done": r.steps_done,
+                "state": w, "energy": e[:nsteps] if we else None}
+
+    def stats(self):
+        i = ServerInfo()
+        _check(lib.am_server_stats(self.h, ctypes.byref(i)), None, "am_server_stats")
+        return {f: getattr(i, f) for f, _ in ServerInfo._fields_}
+
+    def close(self):
+        if self.h:
+            lib.am_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def footprint_bytes(params):
+    return lib.am_footprint_bytes(ctypes.byref(params))
 
 
 def make_params(nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None, dealias="reference",

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC] + ARCH
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 
-CUDA_UNITS = ["actflow_api.cu", "kernels_f32.cu", "kernels_f64.cu", "noalloc.cu", "kernels_batch.cu", "batch.cu"]
+CUDA_UNITS = ["actflow_api.cu", "kernels_f32.cu", "kernels_f64.cu", "noalloc.cu", "kernels_batch.cu", "batch.cu", "ragged.cu", "server.cu"]
 HOST_UNITS = ["spec.cpp", "io.cpp", "driver.cpp", "cli.cpp"]
 
 

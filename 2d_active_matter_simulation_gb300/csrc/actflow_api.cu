@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "actflow.h"
+#include "handle_internal.h"
 #include "host_tables.h"
 #include "kernels.h"
 
@@ -103,20 +104,20 @@ static am_status alloc_and_tables(am_handle *h)
     const size_t stage = (size_t)ny * h->nxh * sizeof(cpx<T>);
     void **fields[] = {&h->u0, &h->acc, &h->fa, &h->fx, &h->fy, &h->P, &h->Q};
     for (void **f : fields) {
-        CK(h, cudaMalloc(f, field));
+        CK(h, cudaMallocAsync(f, field, h->stream));
         CK(h, cudaMemsetAsync(*f, 0, field, h->stream));
         h->bytes += field;
     }
-    CK(h, cudaMalloc(&h->stage, stage));
+    CK(h, cudaMallocAsync(&h->stage, stage, h->stream));
     h->bytes += stage;
-    CK(h, cudaMalloc(&h->twx, nx * sizeof(cpx<T>)));
-    CK(h, cudaMalloc(&h->twy, ny * sizeof(cpx<T>)));
-    CK(h, cudaMalloc(&h->kxt, h->nt * W * sizeof(T)));
-    CK(h, cudaMalloc(&h->kyt, ny * sizeof(T)));
-    CK(h, cudaMalloc(&h->rowp, side_bytes(ny)));
+    CK(h, cudaMallocAsync(&h->twx, nx * sizeof(cpx<T>), h->stream));
+    CK(h, cudaMallocAsync(&h->twy, ny * sizeof(cpx<T>), h->stream));
+    CK(h, cudaMallocAsync(&h->kxt, h->nt * W * sizeof(T), h->stream));
+    CK(h, cudaMallocAsync(&h->kyt, ny * sizeof(T), h->stream));
+    CK(h, cudaMallocAsync(&h->rowp, side_bytes(ny), h->stream));
     CK(h, cudaMemsetAsync(h->rowp, 0, side_bytes(ny), h->stream));
-    CK(h, cudaMalloc(&h->energy, ECAP * sizeof(double)));
-    CK(h, cudaMalloc(&h->sc, sizeof(Scalars)));
+    CK(h, cudaMallocAsync(&h->energy, ECAP * sizeof(double), h->stream));
+    CK(h, cudaMallocAsync(&h->sc, sizeof(Scalars), h->stream));
     h->bytes += nx * sizeof(cpx<T>) + ny * sizeof(cpx<T>) + h->nt * W * sizeof(T) + ny * sizeof(T) +
                 side_bytes(ny) + ECAP * sizeof(double) + sizeof(Scalars);
 
@@ -335,6 +336,30 @@ static am_status step_impl(am_handle *h, int nsteps, double *energy, int *nan_st
     return AM_OK;
 }
 
+// ------------------------------------------- serving-engine hooks (internal)
+
+namespace af {
+
+int handle_ring_capacity() { return ECAP; }
+
+cudaStream_t handle_stream(const am_handle *h) { return h ? h->stream : nullptr; }
+
+am_status handle_enqueue_chunk(am_handle *h, int k, double *energy_host, void *scalars_host, cudaEvent_t done)
+{
+    if (!h || k < 1 || k > ECAP || !scalars_host || !h->state_loaded) return AM_ERR_ARG;
+    am_status st = h->fp64 ? build_graph<double>(h) : build_graph<float>(h);
+    if (st) return st;
+    CK(h, cudaMemsetAsync(&h->sc->step, 0, sizeof(int), h->stream));
+    for (int i = 0; i < k; i++) CK(h, cudaGraphLaunch(h->graph, h->stream));
+    if (energy_host)
+        CK(h, cudaMemcpyAsync(energy_host, h->energy, k * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(scalars_host, h->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaEventRecord(done, h->stream));
+    return AM_OK;
+}
+
+}  // namespace af
+
 // ------------------------------------------------------------------- C ABI
 
 extern "C" {
@@ -350,6 +375,7 @@ const char *am_status_string(am_status s)
     case AM_ERR_SPEC: return "specification error";
     case AM_ERR_OOM: return "out of device memory";
     case AM_ERR_UNSUPPORTED: return "unsupported";
+    case AM_ERR_TIMEOUT: return "timed out";
     }
     return "unknown status";
 }
@@ -398,12 +424,14 @@ am_status am_create(const am_params *p, am_handle **out)
 am_status am_destroy(am_handle *h)
 {
     if (!h) return AM_OK;
-    if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->graph) cudaGraphExecDestroy(h->graph);
+    // Stream-ordered frees: the memory returns to the pool once the handle's
+    // own work is done, without waiting for other streams of the device.
     void *ptrs[] = {h->u0, h->acc, h->fa, h->fx, h->fy, h->P, h->Q, h->stage, h->twx, h->twy,
                     h->kxt, h->kyt, h->rowp, h->energy, h->sc};
     for (void *q : ptrs)
-        if (q) cudaFree(q);
+        if (q) cudaFreeAsync(q, h->stream);
+    if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return AM_OK;
@@ -512,6 +540,19 @@ am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double co
 int am_launches_per_step(const am_handle *h) { return h ? 8 : 0; }
 
 long long am_device_bytes(const am_handle *h) { return h ? h->bytes : 0; }
+
+long long am_footprint_bytes(const am_params *p)
+{
+    if (!p || !is_pow2(p->nx) || !is_pow2(p->ny)) return -1;
+    const bool f64 = p->precision == AM_FP64;
+    const size_t cs = f64 ? sizeof(cpx<double>) : sizeof(cpx<float>), rs = f64 ? sizeof(double) : sizeof(float);
+    const int W = f64 ? Tile<double>::W : Tile<float>::W;
+    const int nxh = p->nx / 2 + 1, nt = (nxh + W - 1) / W;
+    const size_t field = (size_t)nt * W * p->ny * cs;
+    return (long long)(7 * field + (size_t)p->ny * nxh * cs + (size_t)(p->nx + p->ny) * cs +
+                       (size_t)nt * W * rs + (size_t)p->ny * rs + side_bytes(p->ny) + ECAP * sizeof(double) +
+                       sizeof(Scalars));
+}
 
 int am_kx_carried(const am_handle *h)
 {

@@ -161,8 +161,11 @@ struct RowPass {
     static constexpr int BUFS = (Buf::slots(M) + 7) / 8 * 8;   // complex slots per buffer
 
     // per row: two exchange buffers (double buffering) for each of the three
-    // transforms that run in lockstep
-    static constexpr int NBUF = 6;
+    // transforms that run in lockstep; where six do not fit in shared memory
+    // (FP64, Nx = 4096) each transform reuses one buffer for every exchange
+    // (SINGLE: one more barrier per exchange)
+    static constexpr int SINGLE = (size_t)ROWS * 6 * BUFS * sizeof(cpx<T>) > (size_t)227 * 1024 ? 1 : 0;
+    static constexpr int NBUF = SINGLE ? 3 : 6;
     static constexpr size_t smem_bytes() { return (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>); }
 
     // C2R pre-processing of X(k), X(M-k): Z(k) = E + i O with
@@ -334,7 +337,8 @@ struct RowPass {
         const int ny = a.ny;
         cpx<T> *rbase = reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * NBUF * BUFS;
         const Buf b0[3] = {Buf{rbase}, Buf{rbase + BUFS}, Buf{rbase + 2 * BUFS}};
-        const Buf b1[3] = {Buf{rbase + 3 * BUFS}, Buf{rbase + 4 * BUFS}, Buf{rbase + 5 * BUFS}};
+        const Buf b1[3] = {Buf{rbase + (3 - 3 * SINGLE) * BUFS}, Buf{rbase + (4 - 3 * SINGLE) * BUFS},
+                           Buf{rbase + (5 - 3 * SINGLE) * BUFS}};
 
         // ---- C2R along x of uy, ux and w, the three transforms in lockstep
         const cpx<T> wj = ldtw(a.twx, j);
@@ -346,7 +350,7 @@ struct RowPass {
             load_pairs(A, B, src[f], j, y, ny, a.kxp);
             pack_pairs(v[f], A, B, wj, j);
         }
-        FFTi::template run_multi<3>(v, j, 0, b0, b1, a.twx, 2, sync);
+        FFTi::template run_multi<3, SINGLE>(v, j, 0, b0, b1, a.twx, 2, sync);
 
         // ---- real-space products; v[f][r] holds x = 2n (real part) and
         // 2n + 1 (imaginary part), n = j + r * TPC.  P replaces uy, Q replaces ux.
@@ -380,8 +384,8 @@ struct RowPass {
         cpx<T>(&pq)[2][R] = *reinterpret_cast<cpx<T>(*)[2][R]>(&v[0]);
         const Buf pb0[2] = {b0[0], b0[1]};
         const Buf pb1[2] = {b1[0], b1[1]};
-        FFTf::template run_multi<2>(pq, j, 0, pb0, pb1, a.twx, 2, sync);
-        if constexpr (FFTf::NEXCH == 0) sync();
+        FFTf::template run_multi<2, SINGLE>(pq, j, 0, pb0, pb1, a.twx, 2, sync);
+        if constexpr (FFTf::NEXCH == 0 || SINGLE) sync();   // the pairing buffer may still be read
 #pragma unroll
         for (int f = 0; f < 2; f++) {
             const Buf &pb = (FFTf::NEXCH & 1) ? pb1[f] : pb0[f];

@@ -46,13 +46,22 @@ PRESETS = {
     # pass for all members), alpha ~ U[-1, -0.3] and lambda ~ U[2, 5] drawn with
     # numpy's default_rng(2), member seeds 1000 + i.
     2: dict(n=512, dt=2.5e-4, dealias="half", seed=1000, members=64),
+    # --config 3: ragged batch of 40 runs, grids log-uniform over {128..1024}^2,
+    # steps U[1000, 5000], alpha ~ U[-1, -0.3], lambda ~ U[2, 5],
+    # dt = 0.1 dx / sqrt(-alpha / beta); master seed 3, run seeds 2000 + i.
+    3: dict(n=1024, dt=0.0, dealias="half", seed=2000, runs=40),
+    # --config 4: serving trace, Poisson arrivals at 4 requests/s, grids
+    # log-uniform over {128..4096}^2, 10% FP64, steps log-uniform 500..20000,
+    # parameters as config 2; master seed 4.  --serve-seconds sets the arrival
+    # window and --serve-step-scale scales every request's step count.
+    4: dict(n=4096, dt=0.0, dealias="half", seed=4, rate=4.0),
 }
 
 
 def apply_preset(cfg, precision):
     global NX, NY, SEED, PRECISION, WORKLOAD
     p = PRESETS[cfg]
-    if cfg == 2:
+    if cfg in (2, 3):
         precision = "fp32"
     NX = NY = p["n"]
     SEED = p["seed"]
@@ -65,7 +74,7 @@ def apply_preset(cfg, precision):
 
 # DRAM read + write bytes per launch of each pass for this workload, from the
 # ncu capture summarised in profiles/k_row_k_col_2048_fp32_full.md
-NCU_TRAFFIC = {"row": 25.426e6 + 0.402e6, "col": 25.514e6 + 0.551e6}
+NCU_TRAFFIC = {"row": 25.417e6 + 0.058e6, "col": 25.496e6 + 0.193e6}
 
 
 def peaks():
@@ -272,7 +281,7 @@ def run_ours(args):
         n_cpu = 0
         t_cpu = 0.0
         cores = 1
-        while t_cpu < 10.0 and n_cpu < 30:
+        while t_cpu < 10.0 and n_cpu < 200:
             dt, cores = oracle_steps(1)
             t_cpu += dt
             n_cpu += 1
@@ -407,6 +416,154 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def _drawn_params(am, rng, nx, precision="fp32"):
+    """alpha ~ U[-1, -0.3], lambda ~ U[2, 5], beta, Gamma0, Gamma2 as config 0, 2 pi box,
+    dt = 0.1 dx / u_est with u_est = sqrt(-alpha / beta)."""
+    alpha = float(rng.uniform(-1.0, -0.3))
+    lam = float(rng.uniform(2.0, 5.0))
+    dt = 0.1 * (2 * math.pi / nx) / math.sqrt(-alpha / PARAMS["beta"])
+    return am.make_params(nx, nx, PARAMS["lx"], PARAMS["ly"], dt, lam, alpha, PARAMS["beta"],
+                          gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias="half", precision=precision)
+
+
+def run_ragged(args):
+    """Config 3: 40 runs of mixed grids and step counts advanced by one am_ragged
+    to completion; value = all runs' grid-point-steps / wall time of am_ragged_run."""
+    import importlib
+
+    import numpy as np
+    import torch
+
+    am = importlib.import_module("2d_active_matter_simulation_gb300")
+    nr = PRESETS[3]["runs"]
+    rng = np.random.default_rng(3)
+    sizes = [int(2 ** rng.integers(7, 11)) for _ in range(nr)]
+    steps = [int(rng.integers(1000, 5001)) for _ in range(nr)]
+    params = [_drawn_params(am, rng, n) for n in sizes]
+    ics = [am.ic_bandlimited(n, n, 2000 + i).astype(np.complex64) for i, n in enumerate(sizes)]
+    # warm-up: the same runs for `warmup` steps each
+    warm = am.Ragged(params, [max(args.warmup, 1)] * nr)
+    for i in range(nr):
+        warm.set_state(i, ics[i])
+    warm.run(energy=False)
+    warm.close()
+    rg = am.Ragged(params, steps)
+    for i in range(nr):
+        rg.set_state(i, ics[i])
+    clocks = ClockSampler()
+    clocks.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, gps = rg.run(energy=True)
+    dt = time.perf_counter() - t0
+    clk = clocks.stop()
+    classes = rg.classes
+    rg.close()
+    hist = {f"{n}^2": sizes.count(n) for n in sorted(set(sizes))}
+    out = {
+        "metric": "grid-point-steps/s", "value": gps / dt, "unit": "grid-point-steps/s", "n_gpus": 1,
+        "steps": int(sum(steps)), "warmup": args.warmup, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"ragged batch: {nr} runs, grids {hist}, steps U[1000,5000] (total "
+                               f"{sum(steps)} run-steps), per-run dt, 1/2 rule, FP32",
+                   "runs": nr, "size_classes": classes, "seconds": dt, "grid_point_steps": gps,
+                   "timing": "host wall clock around am_ragged_run (one CUDA graph per step with one branch per "
+                             "size class, energies of every run copied back per segment)"},
+        "gpu_launches": _ragged_launches(sizes, steps), "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def _ragged_launches(sizes, steps):
+    """Kernels am_ragged_run launches: per segment (steps up to the next run's
+    end, at most 1024), 8 per step for each size class with active runs, plus
+    one step-counter reset."""
+    done = [0] * len(steps)
+    total = 0
+    while True:
+        act = [i for i in range(len(steps)) if done[i] < steps[i]]
+        if not act:
+            return total
+        k = min(1024, min(steps[i] - done[i] for i in act))
+        total += k * 8 * len({sizes[i] for i in act}) + 1
+        for i in act:
+            done[i] += k
+
+
+def _serving_trace(am, window_s, step_scale, rate, seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t > window_s:
+            return out
+        n = int(2 ** rng.integers(7, 13))
+        fp64 = bool(rng.uniform() < 0.1)
+        steps = int(round(math.exp(rng.uniform(math.log(500), math.log(20000))) * step_scale))
+        p = _drawn_params(am, rng, n, "fp64" if fp64 else "fp32")
+        out.append((t, p, max(steps, 1), int(rng.integers(0, 2 ** 31))))
+
+
+def _serve(am, trace, max_active, order):
+    import numpy as np
+    srv = am.Server(max_active=max_active, chunk_steps=256, order=order)
+    t0 = time.perf_counter()
+    ids = []
+    for t, p, k, sd in trace:
+        delay = t - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(srv.submit(p, k, seed=sd, want_state=False, want_energy=False))
+    res = [srv.wait(i) for i in ids]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat = np.array([r["t_done"] - r["t_submit"] for r in res])
+    bad = [r for r in res if r["status"] != am.AM_OK]
+    gps = sum(p.nx * p.ny * k for _, p, k, _ in trace)
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean()), "gps_per_s": gps / wall, "wall_s": wall, "failed": len(bad),
+            "failures": [f"{trace[ids.index(r['id'])][1].nx}^2 "
+                         f"{'FP64' if trace[ids.index(r['id'])][1].precision else 'FP32'}: {r['error']}"
+                         for r in bad[:3]],
+            "peak_active": st["peak_active"], "peak_device_gb": st["peak_device_bytes"] / 1e9}
+
+
+def run_serving(args):
+    """Config 4: a Poisson request trace through am_server (continuous batching)
+    and, for comparison, through the same engine with one request at a time."""
+    import importlib
+
+    am = importlib.import_module("2d_active_matter_simulation_gb300")
+    pre = PRESETS[4]
+    # warm-up: a few small requests load every kernel once
+    warm = _serving_trace(am, 2.0, 0.002, pre["rate"], 99)
+    _serve(am, [(0.0, p, k, s) for _, p, k, s in warm], 16, "arrival")
+    trace = _serving_trace(am, args.serve_seconds, args.serve_step_scale, pre["rate"], pre["seed"])
+    clocks = ClockSampler()
+    clocks.start()
+    cb = _serve(am, trace, 16, "arrival")
+    clk = clocks.stop()
+    one = _serve(am, trace, 1, "arrival")
+    nfp64 = sum(1 for _, p, _, _ in trace if p.precision == am.FP64)
+    out = {
+        "metric": "served p50/p99 job latency", "value": cb["p50_s"], "unit": "s", "n_gpus": 1,
+        "steps": len(trace), "warmup": len(warm), "ms_per_step": None, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
+        "p50_s": cb["p50_s"], "p99_s": cb["p99_s"], "grid_point_steps_per_s": cb["gps_per_s"],
+        "continuous_batching": cb, "one_at_a_time": one,
+        "config": {"workload": f"serving trace: Poisson {pre['rate']:g}/s over {args.serve_seconds:g} s "
+                               f"({len(trace)} requests, {nfp64} FP64), grids log-uniform 128^2..4096^2, steps "
+                               f"log-uniform 500..20000 scaled by {args.serve_step_scale:g}, 1/2 rule",
+                   "max_active": 16, "chunk_steps": 256, "hbm_budget_gb": 180 * 2 ** 30 / 1e9,
+                   "timing": "latency = result ready - submit, on the server's clock; requests submitted "
+                             "at their arrival times by a host thread"},
+        "gpu_launches": 8 * sum(k for _, _, k, _ in trace), "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -418,6 +575,8 @@ def main():
     ap.add_argument("--acc-steps", type=int, default=20000)
     ap.add_argument("--config", type=int, default=1, choices=sorted(PRESETS))
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--serve-seconds", type=float, default=20.0, help="config 4: arrival window")
+    ap.add_argument("--serve-step-scale", type=float, default=0.05, help="config 4: step-count scale")
     args = ap.parse_args()
     apply_preset(args.config, args.precision)
     if args.accuracy:
@@ -425,6 +584,12 @@ def main():
         return
     if args.config == 2 and args.impl == "ours":
         run_batch(args)
+        return
+    if args.config == 3 and args.impl == "ours":
+        run_ragged(args)
+        return
+    if args.config == 4 and args.impl == "ours":
+        run_serving(args)
         return
     if args.gpus != 1:
         if int(os.environ.get("RANK", "0")) == 0:

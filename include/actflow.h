@@ -38,7 +38,8 @@ typedef enum {
     AM_ERR_IO = 4,           /* file could not be read or written */
     AM_ERR_SPEC = 5,         /* malformed specifications.txt / unknown key */
     AM_ERR_OOM = 6,          /* device allocation failed */
-    AM_ERR_UNSUPPORTED = 7   /* request outside what this build supports */
+    AM_ERR_UNSUPPORTED = 7,  /* request outside what this build supports */
+    AM_ERR_TIMEOUT = 8       /* a wait ran out before the result was ready */
 } am_status;
 
 typedef enum { AM_FP32 = 0, AM_FP64 = 1 } am_precision;
@@ -69,6 +70,7 @@ typedef struct am_params {
 } am_params;
 
 typedef struct am_handle am_handle;
+typedef struct am_server am_server;
 
 /* Allocate device buffers, twiddle and wavenumber tables and the integrating
  * factors for one simulation.  Replaces the reference's set-up
@@ -153,6 +155,99 @@ am_status am_batch_get_state(am_batch *b, int member, void *w_hat, double mean[2
  * values.  AM_ERR_NAN names the first member whose w(0,0) became NaN. */
 am_status am_batch_step(am_batch *b, int nsteps, double *energy, int *nan_member);
 const char *am_batch_last_error(const am_batch *b);
+
+/* ------------------------------------------------------- ragged batches --
+ * A ragged batch advances R simulations of DIFFERENT grid sizes, parameters,
+ * time steps and step counts together.  The reference runs one simulation per
+ * process (its time loop, ActFlow_V3-2.cu:718-862); a ragged batch is that loop
+ * for R independent runs.  Runs are grouped by grid size, largest first; each
+ * pass of a step is one launch per size class over all of its active runs,
+ * and the classes run as parallel branches of one CUDA graph per step.  A run
+ * stops at its own step count.  FP32, grids 128..1024 per axis.  Each run
+ * computes exactly what a handle with its parameters computes. */
+typedef struct am_ragged am_ragged;
+am_status am_ragged_create(const am_params *params /* [nruns] */, const long long *nsteps /* [nruns] */,
+                           int nruns, am_ragged **out);
+am_status am_ragged_destroy(am_ragged *r);
+/* Run state in and out, as am_set_state / am_get_state (host buffers). */
+am_status am_ragged_set_state(am_ragged *r, int run, const void *w_hat, const double mean[2]);
+am_status am_ragged_get_state(am_ragged *r, int run, void *w_hat, double mean[2]);
+/* Advance every run to its step count.  energy, if not NULL, is an array of
+ * nruns pointers, each NULL or receiving nsteps[run] energies.  AM_ERR_NAN
+ * names the first run whose w(0,0) became NaN.  *grid_point_steps receives
+ * the sum of Nx*Ny*steps advanced. */
+am_status am_ragged_run(am_ragged *r, double *const *energy, int *nan_run, long long *grid_point_steps);
+long long am_ragged_device_bytes(const am_ragged *r);
+int am_ragged_classes(const am_ragged *r);
+const char *am_ragged_last_error(const am_ragged *r);
+
+/* ------------------------------------------------------------- serving --
+ * A server takes simulation requests (grid, parameters, precision, seed or
+ * initial state, step count) from any thread and runs them with continuous
+ * batching on one GPU: requests are admitted while their device footprint
+ * fits the HBM budget and an active slot is free, each admitted request
+ * advances in chunks of steps on its own stream (so the kernels of different
+ * requests overlap on the device), and a request that arrives while others run
+ * is admitted as soon as memory and a slot free up.  The reference has no
+ * counterpart (one simulation per process, ActFlow_V3-2.cu:214-878); each
+ * request computes exactly what a lone handle computes. */
+typedef enum { AM_ORDER_ARRIVAL = 0, AM_ORDER_SHORTEST_FIRST = 1 } am_order;
+
+typedef struct am_server_config {
+    long long hbm_budget_bytes;  /* device bytes the admitted requests may hold (0: 180 GiB) */
+    int max_active;              /* requests on the GPU at once (0: 16) */
+    int chunk_steps;             /* largest chunk of steps (0: 256; at most 4096); each request's
+                                    chunks hold about 20 ms of estimated GPU time, up to this */
+    int order;                   /* am_order: admission order of pending requests */
+    int reserved[5];             /* must be zero */
+} am_server_config;
+
+typedef struct am_job {
+    am_params params;
+    long long nsteps;
+    const void *w_hat;           /* initial state [Ny][Nx/2+1] in the params' precision (copied at
+                                    submit), or NULL: the seeded band-limited field below */
+    double mean[2];              /* initial scaled mean velocity */
+    unsigned long long seed;     /* am_ic_bandlimited arguments when w_hat is NULL */
+    double kmin, kmax, rms;
+    int want_state;              /* keep the final w_hat for am_server_wait */
+    int want_energy;             /* keep the energy series for am_server_wait */
+    int reserved[4];             /* must be zero */
+} am_job;
+
+typedef struct am_job_result {
+    long long id;
+    int status;                  /* am_status of the request */
+    double t_submit, t_admit, t_done;   /* seconds since am_server_create */
+    double mean[2];              /* final scaled mean velocity */
+    long long steps_done;
+    char error[256];
+} am_job_result;
+
+typedef struct am_server_info {
+    double elapsed_s;
+    long long jobs_submitted, jobs_done, jobs_pending;
+    int jobs_active, peak_active;
+    long long grid_point_steps;  /* completed requests' Nx*Ny*nsteps */
+    long long device_bytes_reserved, peak_device_bytes;
+} am_server_info;
+
+am_status am_server_create(const am_server_config *cfg /* NULL: defaults */, am_server **out);
+/* Queue a request; *id receives its id.  AM_ERR_OOM if its footprint alone
+ * exceeds the budget, AM_ERR_UNSUPPORTED for a grid the solver does not take. */
+am_status am_server_submit(am_server *s, const am_job *job, long long *id);
+/* Wait up to timeout_s seconds (< 0: no limit) for request `id` and collect
+ * its result (once): res, the final state (w_hat, if want_state) and the
+ * energies (energy, nsteps values, if want_energy).  Returns the request's
+ * status, or AM_ERR_TIMEOUT. */
+am_status am_server_wait(am_server *s, long long id, double timeout_s, am_job_result *res, void *w_hat,
+                         double *energy);
+am_status am_server_stats(am_server *s, am_server_info *out);
+/* Run every queued request to completion, then stop the server. */
+am_status am_server_destroy(am_server *s);
+
+/* Device bytes a handle with these parameters holds (what admission reserves). */
+long long am_footprint_bytes(const am_params *p);
 
 /* Number of kernel launches one step makes (for accounting). */
 int am_launches_per_step(const am_handle *h);

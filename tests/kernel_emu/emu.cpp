@@ -157,6 +157,7 @@ int dispatch_x(int ly, const am_params &p, T *w, double *m, int n, double *e, co
         case 9: return dispatch_y<T, LX, 9>(p, w, m, n, e, real, fwd, mask);
         case 10: return dispatch_y<T, LX, 10>(p, w, m, n, e, real, fwd, mask);
         case 11: return dispatch_y<T, LX, 11>(p, w, m, n, e, real, fwd, mask);
+        case 12: return dispatch_y<T, LX, 12>(p, w, m, n, e, real, fwd, mask);
         }
     }
     return -100;
@@ -188,6 +189,7 @@ int dispatch(const am_params &p, T *w, double *m, int n, double *e, const T *rea
     case 9: return dispatch_long_x<T, 9>(ly, p, w, m, n, e, real, fwd, mask);
     case 10: return dispatch_long_x<T, 10>(ly, p, w, m, n, e, real, fwd, mask);
     case 11: return dispatch_long_x<T, 11>(ly, p, w, m, n, e, real, fwd, mask);
+    case 12: return dispatch_long_x<T, 12>(ly, p, w, m, n, e, real, fwd, mask);
     }
     return -100;
 }
@@ -197,7 +199,7 @@ int dispatch(const am_params &p, T *w, double *m, int n, double *e, const T *rea
 extern "C" {
 // Advance (w_hat [ny][nx/2+1] complex of the precision, mean[2]) nsteps steps.
 // Returns the first NaN step or -1; -100 for an unsupported size (8..128 each,
-// or one side 512..2048 with the other 8..16).
+// or one side 512..4096 with the other 8..16).
 int emu_run(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy)
 {
     if (p->precision == AM_FP64)

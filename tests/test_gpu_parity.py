@@ -113,7 +113,8 @@ def test_gpu_mask512_reference_quirk(am):
     sim.close()
 
 
-@pytest.mark.parametrize("n", [(256, 256), (512, 128), (128, 512), (1024, 1024), (2048, 64), (64, 2048)])
+@pytest.mark.parametrize("n", [(256, 256), (512, 128), (128, 512), (1024, 1024), (2048, 64), (64, 2048),
+                               (4096, 64), (64, 4096)])
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
 @pytest.mark.parametrize("dealias", ["reference", "half"])
 def test_gpu_sizes_vs_oracle(am, orc, n, prec, dealias):

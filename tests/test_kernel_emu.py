@@ -104,12 +104,14 @@ def test_emulated_pruned_half_rule(am, orc, emu, n, prec):
     assert np.abs(w[mask == 0]).max() == 0.0
 
 
-@pytest.mark.parametrize("n", [(2048, 16), (16, 2048)])
+@pytest.mark.parametrize("n,kind", [((2048, 16), "full"), ((2048, 16), "pruned"), ((16, 2048), "full"),
+                                    ((16, 2048), "pruned"), ((4096, 8), "full"), ((8, 4096), "full")])
 @pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("kind", ["full", "pruned"])
 def test_emulated_production_lengths(am, orc, emu, n, prec, kind):
     """The row kernel at Nx = 2048 and the column kernel at Ny = 2048 (the
-    benchmark's transform lengths), with few rows or columns so that the
+    benchmark's transform lengths) and at 4096 (the largest grid: the FP64 row
+    pass there reuses one exchange buffer per transform, and the column pass
+    runs its transforms one at a time), with few rows or columns so that the
     emulation stays quick.  A unit-variance white-noise field and dt = 1e-3
     make the nonlinear term about 1e-3 of the result, so FP64 agreement to
     1e-13 pins the nonlinear term to about 1e-10.  "pruned": the state is

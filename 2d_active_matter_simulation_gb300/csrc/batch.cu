@@ -212,6 +212,10 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
         if (csm > 48 * 1024 &&
             cudaFuncSetAttribute((const void *)KB.col[ly][m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm))
             return fail(AM_ERR_CUDA);
+    // am_batch_set_state starts a member with the single-simulation stage-0 kernel
+    if (csm > 48 * 1024 &&
+        cudaFuncSetAttribute((const void *)K.col[ly][0], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm))
+        return fail(AM_ERR_CUDA);
     *out = b;
     return AM_OK;
 }

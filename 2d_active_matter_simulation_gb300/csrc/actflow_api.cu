@@ -171,7 +171,7 @@ static am_status launch_col(am_handle *h, int mode)
     StepArgs<T> a = args_of<T>(h);
     a.mode = mode;
     const LaunchShape &s = K.col_shape[h->logny];
-    int grid = (a.ntp + s.per_block - 1) / s.per_block;
+    int grid = col_grid(s, a.ntp, Tile<T>::W);
     K.col[h->logny][mode]<<<grid, s.threads, s.smem, h->stream>>>(a);
     CK(h, cudaGetLastError());
     return AM_OK;

@@ -93,7 +93,7 @@ am_status build_graph(am_batch *b)
     const LaunchShape &rs = K.row_shape[b->lognx];
     const LaunchShape &cs = K.col_shape[b->logny];
     const dim3 rgrid((b->ny + rs.per_block - 1) / rs.per_block, b->B);
-    const dim3 cgrid((ntp + cs.per_block - 1) / cs.per_block, b->B);
+    const dim3 cgrid(col_grid(cs, ntp, Tile<float>::W), b->B);
     cudaGraph_t g;
     BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 1; s <= 4; s++) {
@@ -252,7 +252,7 @@ am_status am_batch_set_state(am_batch *b, int member, const void *w_hat, const d
     StepArgs<float> a0 = a;
     set_pruning<float>(a0, false);
     const LaunchShape &cs = K.col_shape[b->logny];
-    K.col[b->logny][0]<<<(a0.ntp + cs.per_block - 1) / cs.per_block, cs.threads, cs.smem, b->stream>>>(a0);
+    K.col[b->logny][0]<<<col_grid(cs, a0.ntp, Tile<float>::W), cs.threads, cs.smem, b->stream>>>(a0);
     BK(cudaGetLastError());
     BK(cudaStreamSynchronize(b->stream));
     b->inside[member] = state_inside_half_mask<float>((const float *)w_hat, b->nx, b->ny);

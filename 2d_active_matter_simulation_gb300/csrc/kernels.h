@@ -14,8 +14,12 @@ constexpr int LOG_MAX = 12;   // 4096
 struct LaunchShape {
     int threads = 0;
     size_t smem = 0;
-    int per_block = 0;        // rows (row kernels) or column tiles (column kernels) per CTA
+    int per_block = 0;        // rows (row kernels), columns (step column kernels) or column
+                              // tiles (set-up column kernels) per CTA
 };
+
+// CTAs of a step column-pass launch over ntp column tiles of W columns.
+inline int col_grid(const LaunchShape &s, int ntp, int W) { return (ntp * W + s.per_block - 1) / s.per_block; }
 
 template <typename T>
 struct KernelTable {

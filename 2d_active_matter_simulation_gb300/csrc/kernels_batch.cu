@@ -13,7 +13,8 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
 }
 
 template <typename T, int LOG, int MODE>
-__global__ void __launch_bounds__(ColPass<T, LOG, MODE>::THREADS) k_col_b(const StepArgs<T> *__restrict__ args)
+__global__ void __launch_bounds__(ColPass<T, LOG, MODE>::THREADS, ColPass<T, LOG, MODE>::MINB)
+    k_col_b(const StepArgs<T> *__restrict__ args)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const StepArgs<T> a = args[blockIdx.y];

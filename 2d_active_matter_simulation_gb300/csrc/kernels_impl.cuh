@@ -14,7 +14,7 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
 }
 
 template <typename T, int LOG, int MODE>
-__global__ void __launch_bounds__(ColPass<T, LOG, MODE>::THREADS) k_col(StepArgs<T> a)
+__global__ void __launch_bounds__(ColPass<T, LOG, MODE>::THREADS, ColPass<T, LOG, MODE>::MINB) k_col(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     ColPass<T, LOG, MODE>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
@@ -75,7 +75,7 @@ struct Fill {
         t.col[LOG][2] = k_col<T, LOG, 2>;
         t.col[LOG][3] = k_col<T, LOG, 3>;
         t.col[LOG][4] = k_col<T, LOG, 4>;
-        t.col_shape[LOG] = {ColPass<T, LOG, 1>::THREADS, ColPass<T, LOG, 1>::smem_bytes(), ColPass<T, LOG, 1>::TILES};
+        t.col_shape[LOG] = {ColPass<T, LOG, 1>::THREADS, ColPass<T, LOG, 1>::smem_bytes(), ColPass<T, LOG, 1>::COLS};
         t.rowfwd[LOG] = k_rowfwd<T, LOG>;
         t.rowfwd_shape[LOG] = {RowFwd<T, LOG>::THREADS, RowFwd<T, LOG>::smem_bytes(), RowFwd<T, LOG>::ROWS};
         t.colfwd[LOG] = k_colfwd<T, LOG>;

@@ -193,7 +193,7 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
     k_mean<<<1, 1, 0, st>>>(a.sc, mean, 1);
     K.tile<<<1024, 256, 0, st>>>((const cpx<T> *)w_hat, a.u0, ny, nxh, nt);
     const int rgrid = (ny + rs.per_block - 1) / rs.per_block;
-    const int cgrid = (nt + cs.per_block - 1) / cs.per_block;
+    const int cgrid = col_grid(cs, nt, Tile<T>::W);
     StepArgs<T> b = a;
     b.mode = 0;
     K.col[ly2][0]<<<cgrid, cs.threads, cs.smem, st>>>(b);

@@ -181,7 +181,7 @@ am_status rebuild(am_ragged *r, const std::vector<char> &act)
         const int ny = 1 << c.logny;
         const int nb = (int)c.active.size();
         const dim3 rgrid((ny + rs.per_block - 1) / rs.per_block, nb);
-        const dim3 cgrid((c.ntp + cs.per_block - 1) / cs.per_block, nb);
+        const dim3 cgrid(col_grid(cs, c.ntp, Tile<float>::W), nb);
         const StepArgs<float> *args = r->dargs + c.off;
         for (int s = 1; s <= 4; s++) {
             KB.row[c.lognx]<<<rgrid, rs.threads, rs.smem, c.branch>>>(args);
@@ -370,7 +370,7 @@ am_status am_ragged_set_state(am_ragged *r, int run, const void *w_hat, const do
     StepArgs<float> a0 = R.a;
     set_pruning<float>(a0, false);
     const LaunchShape &cs = K.col_shape[r->cls[R.cls].logny];
-    K.col[r->cls[R.cls].logny][0]<<<(a0.ntp + cs.per_block - 1) / cs.per_block, cs.threads, cs.smem, r->stream>>>(a0);
+    K.col[r->cls[R.cls].logny][0]<<<col_grid(cs, a0.ntp, Tile<float>::W), cs.threads, cs.smem, r->stream>>>(a0);
     RK(cudaGetLastError());
     RK(cudaStreamSynchronize(r->stream));
     R.inside = state_inside_half_mask<float>((const float *)w_hat, R.p.nx, R.p.ny);

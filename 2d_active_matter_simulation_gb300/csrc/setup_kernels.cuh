@@ -57,9 +57,11 @@ struct RowFwd {
 template <typename T, int LOGNY>
 struct ColFwd {
     using CP = ColPass<T, LOGNY, 0>;
-    static constexpr int W = CP::W, R = CP::R, TPC = CP::TPC, TILES = CP::TILES, THREADS = CP::THREADS;
-    static constexpr int BUFS = CP::BUFS;
-    using Buf = typename CP::Buf;
+    // one tile of W columns per group of W * TPC threads
+    static constexpr int W = Tile<T>::W, R = CP::R, TPC = CP::TPC;
+    static constexpr int TILES = W * TPC >= 128 ? 1 : 128 / (W * TPC), THREADS = TILES * W * TPC;
+    using Buf = XBuf<T, W, 0>;
+    static constexpr int BUFS = (Buf::slots(CP::L) + 7) / 8 * 8;
     using FFTf = typename CP::FFTf;
     static constexpr size_t smem_bytes() { return (size_t)TILES * BUFS * sizeof(cpx<T>); }
 

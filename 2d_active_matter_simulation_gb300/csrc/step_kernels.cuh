@@ -507,11 +507,18 @@ AF_HD void cp_async_wait_all()
 }
 
 // --------------------------------------------------------------- column pass
-// One tile of W adjacent kx columns per group of W * TPC threads (lane c =
-// column inside the tile, j = thread of that column's transform), so every
-// warp access to the tile is one contiguous block.  MODE 0 starts from u0
-// (after set_state), MODE 1..4 is the RK stage.
-// Launch: blockDim = TILES * W * TPC, gridDim = ceil(nt / TILES).
+// CW adjacent kx columns per group of CW * TPC threads (lane c = column in the
+// group, j = thread of that column's transform), TILES groups per CTA.
+//  * Ny >= 2048: CW = W, a whole tile per group, so every store covers whole
+//    32-byte sectors (one CTA of 512 threads per SM; FP32 at Ny = 4096 takes
+//    half a tile, 512 threads, to stay within 128 registers).
+//  * Ny <= 1024: CW = 1, one column per group: CTAs of 128 threads, up to four
+//    per SM, each synchronising only its own warps.  Stores then cover a
+//    quarter sector each, which at 2048 cost more (ncu: 4x the L2 write
+//    sectors, 36 -> 47 us) than the extra CTAs won; below it the smaller
+//    CTAs win (ragged batch of 128^2..1024^2 grids +14%).
+// MODE 0 starts from u0 (after set_state), MODE 1..4 is the RK stage.
+// Launch: blockDim = THREADS, gridDim = ceil(columns carried / COLS).
 template <typename T, int LOGNY, int MODE>
 struct ColPass {
     static constexpr int W = Tile<T>::W;
@@ -521,26 +528,37 @@ struct ColPass {
     static constexpr int R = FFTf::R;
     static constexpr int TPC = FFTf::TPC;
     static constexpr int L = 1 << LOGNY;
-    static constexpr int TILES = W * TPC >= 128 ? 1 : 128 / (W * TPC);
-    static constexpr int THREADS = TILES * W * TPC;
-    using Buf = XBuf<T, W, 0>;
+    static constexpr int CW = L < 2048 ? 1 : (W * TPC <= 512 ? W : (512 / TPC > 1 ? 512 / TPC : 1));
+    static constexpr int TILES = CW * TPC >= 128 ? 1 : 128 / (CW * TPC);   // column groups per CTA
+    static constexpr int THREADS = TILES * CW * TPC;
+    static constexpr int COLS = TILES * CW;                                // columns per CTA
+    // CTAs per SM the registers allow (128 per thread at most)
+    static constexpr int MINB = THREADS >= 512 ? 1 : (512 / THREADS > 4 ? 4 : 512 / THREADS);
+    // exchange slots: CW columns interleaved, idx + idx/8; one column: idx +
+    // idx/16 (FP32) / idx + idx/8 (FP64), conflict-free for every pass of
+    // these transforms (simulated bank pattern)
+    using Buf = XBuf<T, CW, (CW == 1 && sizeof(T) == 4) ? 3 : 0>;
     static constexpr int BUFS = (Buf::slots(L) + 7) / 8 * 8;
-    // Shared memory: the exchange buffers; then what CTA 0 fetches at kernel
-    // start in stages 1-4 so that its extra serial work (the mean flow, the
-    // energy, the Hermitian repair) runs from shared memory: the Scalars, the
-    // source of the kx = 0 column's mirror values, the row sums; then one
-    // partial sum per warp.  The fetches are made only where they fit.
+    // Shared memory, within MINB CTAs per SM: the exchange buffers; then what
+    // CTA 0 fetches at kernel start in stages 1-4 so that its extra serial
+    // work (the mean flow, the energy, the Hermitian repair) runs from shared
+    // memory: the Scalars, the row sums, the source of the kx = 0 column's
+    // mirror values (in that order of priority, each where it fits); then one
+    // partial sum per warp.
     static constexpr size_t XB = (size_t)TILES * BUFS * sizeof(cpx<T>);
     static constexpr size_t SCB = sizeof(Scalars);
     static constexpr size_t MIB = (size_t)L * sizeof(cpx<T>);
     static constexpr size_t PFB = (size_t)3 * L * sizeof(T);
-    static constexpr int NW = THREADS / 32;
+    static constexpr int NW = THREADS / 32 > 0 ? THREADS / 32 : 1;
     static constexpr size_t WPB = (size_t)3 * NW * sizeof(RowAcc<T>);
-    static constexpr size_t LIM = (size_t)227 * 1024;
-    static constexpr bool PM = XB + SCB + MIB + WPB <= LIM;              // Scalars + mirror column
-    static constexpr bool PF = PM && XB + SCB + MIB + PFB + WPB <= LIM;  // + row sums
-    static constexpr size_t O_SC = XB, O_MI = XB + SCB, O_PF = O_MI + (PM ? MIB : 0);
-    static constexpr size_t O_WP = O_PF + (PF ? PFB : 0);
+    static constexpr size_t LIM = (size_t)228 * 1024 / MINB - 1024 < (size_t)227 * 1024
+                                      ? (size_t)228 * 1024 / MINB - 1024
+                                      : (size_t)227 * 1024;
+    static constexpr bool PS = XB + SCB + WPB <= LIM;                     // Scalars
+    static constexpr bool PF = PS && XB + SCB + PFB + WPB <= LIM;         // + row sums
+    static constexpr bool PM = PF && XB + SCB + PFB + MIB + WPB <= LIM;   // + mirror column
+    static constexpr size_t O_SC = XB, O_PF = O_SC + SCB, O_MI = O_PF + (PF ? PFB : 0);
+    static constexpr size_t O_WP = O_MI + (PM ? MIB : 0);
     static constexpr int CE = 16 / (int)sizeof(T);                     // row sums per 16-byte copy
 
     static constexpr size_t smem_bytes() { return O_WP + WPB; }
@@ -548,12 +566,12 @@ struct ColPass {
     template <class Sync>
     static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync)
     {
-        const int tl = tid / (W * TPC);
-        const int rem = tid % (W * TPC);
-        const int c = rem % W, j = rem / W;
-        const int tile = bid * TILES + tl;
-        const bool active = tile < a.ntp;
-        const int kx = tile * W + c;
+        const int tl = tid / (CW * TPC);
+        const int rem = tid % (CW * TPC);
+        const int c = rem % CW, j = rem / CW;
+        const int kx = (bid * TILES + tl) * CW + c;   // this thread's column
+        const bool active = kx < a.ntp * W;
+        const int tile = kx / W;                  // its tile in the HBM layout
         const bool col = active && kx <= a.kxp;   // a column that carries data
         const int ny = a.ny, nx = a.nx;
         Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)tl * BUFS};
@@ -563,7 +581,7 @@ struct ColPass {
         RowAcc<T> *wp = reinterpret_cast<RowAcc<T> *>(smem + O_WP);   // warp partials
         const bool owner = bid == 0;   // this CTA holds column kx = 0
         const T kxv = active ? a.kxt[kx] : (T)0;
-        const size_t cbase = active ? (size_t)tile * ny * W + c : 0;
+        const size_t cbase = active ? (size_t)tile * ny * W + kx % W : 0;
         const T dt = a.dt;
         // The kx = 0 column keeps w_new in a.hcol: stage 1 writes half 0,
         // stage 2 reads 0 and writes 1, stage 3 reads 1 and writes 0, stage 4
@@ -576,15 +594,15 @@ struct ColPass {
         // the threads that copied them; the Scalars are read by thread 0, which
         // copied them; the mirror column is read by other threads after the
         // barrier at the start of the second forward transform.
-        if constexpr (MODE != 0 && PM) {
+        if constexpr (MODE != 0 && PS) {
             if (owner) {
                 if (tid < 4) cp_async16(smem + O_SC + 16 * tid, reinterpret_cast<const unsigned char *>(a.sc) + 16 * tid);
-                if constexpr (MODE == 1) {   // w_old of the kx = 0 column (tile 0, lane 0)
+                if constexpr (PM && MODE == 1) {   // w_old of the kx = 0 column (tile 0, lane 0)
                     for (int y = tid; y < ny; y += THREADS) {
                         if constexpr (sizeof(cpx<T>) == 8) cp_async8(mir + y, a.u0 + (size_t)y * W);
                         else cp_async16(mir + y, a.u0 + (size_t)y * W);
                     }
-                } else {
+                } else if constexpr (PM) {
                     constexpr int CC = 16 / (int)sizeof(cpx<T>);
                     for (int q = tid; q < ny / CC; q += THREADS) cp_async16(mir + q * CC, hin + q * CC);
                 }
@@ -609,7 +627,7 @@ struct ColPass {
             for (int r = 0; r < R; r++) ph[r] = v[r];
 #pragma unroll
             for (int r = 0; r < R; r++) v[r] = active ? a.Q[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
-            if constexpr (PM) {
+            if constexpr (PS) {
                 // the owner's copies are complete; the barrier that starts the
                 // next transform makes them visible to the whole CTA
                 if (owner) {
@@ -669,7 +687,7 @@ struct ColPass {
             }
             block_sum3(sum, tid, wp, sync);
             if (tid == 0) {
-                Scalars s = (MODE != 0 && PM) ? *ssm : *a.sc;
+                Scalars s = (MODE != 0 && PS) ? *ssm : *a.sc;
                 const double red[3] = {sum[0].value(), sum[1].value(), sum[2].value()};
                 // Mean-flow right-hand side -beta' Re F[|u|^2 u](0)
                 // (ActFlow_V3-2.cu:1086-1087) and its stage updates

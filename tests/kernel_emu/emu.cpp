@@ -67,7 +67,7 @@ struct Runner {
         auto col = [&](int mode) {
             auto go = [&](auto tag) {
                 using CP = ColPass<T, LY, decltype(tag)::value>;
-                launch((a.ntp + CP::TILES - 1) / CP::TILES, CP::THREADS, CP::smem_bytes(),
+                launch((a.ntp * Tile<T>::W + CP::COLS - 1) / CP::COLS, CP::THREADS, CP::smem_bytes(),
                        [&](int tid, int bid, unsigned char *sm, auto &sync) { CP::body(a, tid, bid, sm, sync); });
             };
             switch (mode) {

@@ -139,6 +139,9 @@ def _load():
         "am_server_stats": ([hp, ctypes.POINTER(ServerInfo)], ctypes.c_int),
         "am_server_destroy": ([hp], ctypes.c_int),
         "am_footprint_bytes": ([ctypes.POINTER(Params)], ctypes.c_longlong),
+        "am_set_column_shape": ([ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "am_column_shape": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "am_autotune": ([ctypes.POINTER(Params), ctypes.c_int, dp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -160,7 +163,7 @@ EXPORTED = [
     "am_ragged_create", "am_ragged_destroy", "am_ragged_set_state", "am_ragged_get_state", "am_ragged_run",
     "am_ragged_device_bytes", "am_ragged_classes", "am_ragged_last_error",
     "am_server_create", "am_server_submit", "am_server_wait", "am_server_stats", "am_server_destroy",
-    "am_footprint_bytes",
+    "am_footprint_bytes", "am_set_column_shape", "am_column_shape", "am_autotune",
 ]
 
 
@@ -426,6 +429,30 @@ class Server:
 
 def footprint_bytes(params):
     return lib.am_footprint_bytes(ctypes.byref(params))
+
+
+COLUMN_SHAPES = ("wide", "narrow")
+
+
+def set_column_shape(precision, ny, shape):
+    """Column-pass launch shape for new simulations of this precision and Ny."""
+    prec = FP64 if precision in ("fp64", FP64) else FP32
+    _check(lib.am_set_column_shape(prec, ny, COLUMN_SHAPES.index(shape) if isinstance(shape, str) else int(shape)),
+           None, "am_set_column_shape")
+
+
+def column_shape(precision, ny):
+    prec = FP64 if precision in ("fp64", FP64) else FP32
+    v = lib.am_column_shape(prec, ny)
+    return COLUMN_SHAPES[v] if v >= 0 else None
+
+
+def autotune(params, nsteps=20):
+    """Time both column-pass shapes for `params` on this GPU, keep the faster.
+    Returns (ms per step wide, ms per step narrow, chosen shape)."""
+    ms = np.zeros(2)
+    _check(lib.am_autotune(ctypes.byref(params), int(nsteps), _dptr(ms)), None, "am_autotune")
+    return float(ms[0]), float(ms[1]), column_shape(params.precision, params.ny)
 
 
 def make_params(nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None, dealias="reference",

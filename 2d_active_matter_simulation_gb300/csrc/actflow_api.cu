@@ -11,6 +11,7 @@
 // CUDA graph and replayed.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -44,6 +45,7 @@ int ilog2(int n)
 struct am_handle {
     am_params p{};
     int nxh = 0, nt = 0, W = 0, lognx = 0, logny = 0;
+    int colv = 0;                  // column-pass launch shape (0 wide, 1 narrow)
     bool fp64 = false;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -150,11 +152,11 @@ static am_status alloc_and_tables(am_handle *h)
         const void *fn;
         size_t smem;
     } ks[] = {{(const void *)K.row[h->lognx], K.row_shape[h->lognx].smem},
-              {(const void *)K.col[h->logny][0], K.col_shape[h->logny].smem},
-              {(const void *)K.col[h->logny][1], K.col_shape[h->logny].smem},
-              {(const void *)K.col[h->logny][2], K.col_shape[h->logny].smem},
-              {(const void *)K.col[h->logny][3], K.col_shape[h->logny].smem},
-              {(const void *)K.col[h->logny][4], K.col_shape[h->logny].smem},
+              {(const void *)K.col[h->logny][h->colv][0], K.col_shape[h->logny][h->colv].smem},
+              {(const void *)K.col[h->logny][h->colv][1], K.col_shape[h->logny][h->colv].smem},
+              {(const void *)K.col[h->logny][h->colv][2], K.col_shape[h->logny][h->colv].smem},
+              {(const void *)K.col[h->logny][h->colv][3], K.col_shape[h->logny][h->colv].smem},
+              {(const void *)K.col[h->logny][h->colv][4], K.col_shape[h->logny][h->colv].smem},
               {(const void *)K.rowfwd[h->lognx], K.rowfwd_shape[h->lognx].smem},
               {(const void *)K.colfwd[h->logny], K.colfwd_shape[h->logny].smem}};
     for (auto &k : ks) {
@@ -170,9 +172,9 @@ static am_status launch_col(am_handle *h, int mode)
     const KernelTable<T> &K = table<T>();
     StepArgs<T> a = args_of<T>(h);
     a.mode = mode;
-    const LaunchShape &s = K.col_shape[h->logny];
+    const LaunchShape &s = K.col_shape[h->logny][h->colv];
     int grid = col_grid(s, a.ntp, Tile<T>::W);
-    K.col[h->logny][mode]<<<grid, s.threads, s.smem, h->stream>>>(a);
+    K.col[h->logny][h->colv][mode]<<<grid, s.threads, s.smem, h->stream>>>(a);
     CK(h, cudaGetLastError());
     return AM_OK;
 }
@@ -336,6 +338,41 @@ static am_status step_impl(am_handle *h, int nsteps, double *energy, int *nan_st
     return AM_OK;
 }
 
+// ------------------------------------------------ column-pass launch shapes
+
+namespace af {
+
+namespace {
+// [fp64][log2 Ny]: 0 wide, 1 narrow; seeded with the measured rule
+std::atomic<int> g_colv[2][LOG_MAX + 1] = {
+    {{1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {0}, {0}},
+    {{1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {0}, {0}}};
+static_assert(LOG_MAX == 12, "seed table covers log2 Ny = 0..12");
+}  // namespace
+
+int col_variant(bool fp64, int logny) { return g_colv[fp64 ? 1 : 0][logny].load(std::memory_order_relaxed); }
+void set_col_variant(bool fp64, int logny, int v) { g_colv[fp64 ? 1 : 0][logny].store(v ? 1 : 0); }
+
+}  // namespace af
+
+// Switch a handle to column-pass shape v (kernel attributes, step graph).
+template <typename T>
+static am_status use_col_variant(am_handle *h, int v)
+{
+    const KernelTable<T> &K = table<T>();
+    const LaunchShape &cs = K.col_shape[h->logny][v];
+    for (int m = 0; m < 5; m++)
+        if (cs.smem > 48 * 1024)
+            CK(h, cudaFuncSetAttribute((const void *)K.col[h->logny][v][m],
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cs.smem));
+    if (h->colv != v && h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    h->colv = v;
+    return AM_OK;
+}
+
 // ------------------------------------------- serving-engine hooks (internal)
 
 namespace af {
@@ -406,6 +443,7 @@ am_status am_create(const am_params *p, am_handle **out)
     h->fp64 = p->precision == AM_FP64;
     h->lognx = ilog2(p->nx);
     h->logny = ilog2(p->ny);
+    h->colv = col_variant(h->fp64, h->logny);
     cudaGetDevice(&h->device);
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete h;
@@ -534,6 +572,69 @@ am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double co
         }
     }
     for (auto &e : ev) cudaEventDestroy(e);
+    return st;
+}
+
+am_status am_set_column_shape(int precision, int ny, int shape)
+{
+    if (!is_pow2(ny) || ny < (1 << LOG_MIN) || ny > (1 << LOG_MAX) || (shape != 0 && shape != 1) ||
+        (precision != AM_FP32 && precision != AM_FP64))
+        return AM_ERR_ARG;
+    set_col_variant(precision == AM_FP64, ilog2(ny), shape);
+    return AM_OK;
+}
+
+int am_column_shape(int precision, int ny)
+{
+    if (!is_pow2(ny) || ny < (1 << LOG_MIN) || ny > (1 << LOG_MAX) ||
+        (precision != AM_FP32 && precision != AM_FP64))
+        return -1;
+    return col_variant(precision == AM_FP64, ilog2(ny));
+}
+
+am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[2])
+{
+    if (!p || nsteps < 1) return AM_ERR_ARG;
+    am_handle *h = nullptr;
+    am_status st = am_create(p, &h);
+    if (st) return st;
+    // a seeded band-limited state in the handle's precision
+    const size_t n = (size_t)p->ny * (p->nx / 2 + 1) * 2;
+    std::vector<double> w(n);
+    st = am_ic_bandlimited(p->nx, p->ny, 1, 1.0, 8.0, 0.01, w.data());
+    std::vector<float> wf;
+    if (!st && p->precision == AM_FP32) {
+        wf.resize(n);
+        for (size_t i = 0; i < n; i++) wf[i] = (float)w[i];
+    }
+    if (!st) st = am_set_state(h, p->precision == AM_FP32 ? (const void *)wf.data() : (const void *)w.data(), nullptr);
+    double best = 0;
+    int bestv = h ? h->colv : 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!st && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) st = AM_ERR_CUDA;
+    for (int v = 0; v < 2 && !st; v++) {
+        st = h->fp64 ? use_col_variant<double>(h, v) : use_col_variant<float>(h, v);
+        if (!st) st = am_step(h, 2, nullptr, nullptr);   // warm-up, builds the graph
+        if (st) break;
+        if (cudaEventRecord(e0, h->stream) != cudaSuccess) st = AM_ERR_CUDA;
+        for (int i = 0; i < nsteps && !st; i++)
+            if (cudaGraphLaunch(h->graph, h->stream) != cudaSuccess) st = AM_ERR_CUDA;
+        float ms = 0;
+        if (!st && (cudaEventRecord(e1, h->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                    cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+            st = AM_ERR_CUDA;
+        if (st) break;
+        const double per = (double)ms / nsteps;
+        if (ms_per_step) ms_per_step[v] = per;
+        if (v == 0 || per < best) {
+            best = per;
+            bestv = v;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    am_destroy(h);
+    if (!st) set_col_variant(p->precision == AM_FP64, ilog2(p->ny), bestv);
     return st;
 }
 

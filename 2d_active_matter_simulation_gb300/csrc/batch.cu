@@ -32,6 +32,7 @@ constexpr int ECAP_B = 1024;   // energy ring entries per member
 struct am_batch {
     std::vector<am_params> p;
     int B = 0, nx = 0, ny = 0, nxh = 0, nt = 0, lognx = 0, logny = 0;
+    int colv = 0;                   // column-pass launch shape (0 wide, 1 narrow)
     cudaStream_t stream = nullptr;
     size_t field_elems = 0;
     cpx<float> *fields = nullptr;   // [B][7][field]
@@ -91,14 +92,14 @@ am_status build_graph(am_batch *b)
     const KernelTable<float> &K = kernels_f32();
     const BatchTable &KB = kernels_batch_f32();
     const LaunchShape &rs = K.row_shape[b->lognx];
-    const LaunchShape &cs = K.col_shape[b->logny];
+    const LaunchShape &cs = K.col_shape[b->logny][b->colv];
     const dim3 rgrid((b->ny + rs.per_block - 1) / rs.per_block, b->B);
     const dim3 cgrid(col_grid(cs, ntp, Tile<float>::W), b->B);
     cudaGraph_t g;
     BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 1; s <= 4; s++) {
         KB.row[b->lognx]<<<rgrid, rs.threads, rs.smem, b->stream>>>(b->dargs);
-        KB.col[b->logny][s]<<<cgrid, cs.threads, cs.smem, b->stream>>>(b->dargs);
+        KB.col[b->logny][b->colv][s]<<<cgrid, cs.threads, cs.smem, b->stream>>>(b->dargs);
     }
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (e != cudaSuccess) {
@@ -149,6 +150,7 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
     b->ny = p0.ny;
     b->lognx = lx;
     b->logny = ly;
+    b->colv = col_variant(false, ly);
     b->loaded.assign(nmembers, 0);
     b->inside.assign(nmembers, 0);
     auto fail = [&](am_status s) {
@@ -204,17 +206,17 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
     // Large shared-memory opt-in for the batched kernels (same sizes as the single ones).
     const KernelTable<float> &K = kernels_f32();
     const BatchTable &KB = kernels_batch_f32();
-    const size_t rsm = K.row_shape[lx].smem, csm = K.col_shape[ly].smem;
+    const size_t rsm = K.row_shape[lx].smem, csm = K.col_shape[ly][b->colv].smem;
     if (rsm > 48 * 1024 &&
         cudaFuncSetAttribute((const void *)KB.row[lx], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm))
         return fail(AM_ERR_CUDA);
     for (int m = 0; m < 5; m++)
         if (csm > 48 * 1024 &&
-            cudaFuncSetAttribute((const void *)KB.col[ly][m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm))
+            cudaFuncSetAttribute((const void *)KB.col[ly][b->colv][m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm))
             return fail(AM_ERR_CUDA);
     // am_batch_set_state starts a member with the single-simulation stage-0 kernel
     if (csm > 48 * 1024 &&
-        cudaFuncSetAttribute((const void *)K.col[ly][0], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm))
+        cudaFuncSetAttribute((const void *)K.col[ly][b->colv][0], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm))
         return fail(AM_ERR_CUDA);
     *out = b;
     return AM_OK;
@@ -251,8 +253,8 @@ am_status am_batch_set_state(am_batch *b, int member, const void *w_hat, const d
     // way the batch is pruned later).
     StepArgs<float> a0 = a;
     set_pruning<float>(a0, false);
-    const LaunchShape &cs = K.col_shape[b->logny];
-    K.col[b->logny][0]<<<col_grid(cs, a0.ntp, Tile<float>::W), cs.threads, cs.smem, b->stream>>>(a0);
+    const LaunchShape &cs = K.col_shape[b->logny][b->colv];
+    K.col[b->logny][b->colv][0]<<<col_grid(cs, a0.ntp, Tile<float>::W), cs.threads, cs.smem, b->stream>>>(a0);
     BK(cudaGetLastError());
     BK(cudaStreamSynchronize(b->stream));
     b->inside[member] = state_inside_half_mask<float>((const float *)w_hat, b->nx, b->ny);

@@ -25,8 +25,8 @@ template <typename T>
 struct KernelTable {
     void (*row[LOG_MAX + 1])(StepArgs<T>);
     LaunchShape row_shape[LOG_MAX + 1];
-    void (*col[LOG_MAX + 1][5])(StepArgs<T>);   // [log2 Ny][mode]
-    LaunchShape col_shape[LOG_MAX + 1];
+    void (*col[LOG_MAX + 1][2][5])(StepArgs<T>);   // [log2 Ny][shape: 0 wide, 1 narrow][mode]
+    LaunchShape col_shape[LOG_MAX + 1][2];
     void (*rowfwd[LOG_MAX + 1])(const T *, cpx<T> *, const cpx<T> *, int, int);
     LaunchShape rowfwd_shape[LOG_MAX + 1];
     void (*colfwd[LOG_MAX + 1])(const cpx<T> *, cpx<T> *, const cpx<T> *, int, int, int, int, int, int, int);
@@ -46,8 +46,14 @@ constexpr int BATCH_LOG_MAX = 10;
 
 struct BatchTable {
     void (*row[LOG_MAX + 1])(const StepArgs<float> *);
-    void (*col[LOG_MAX + 1][5])(const StepArgs<float> *);
+    void (*col[LOG_MAX + 1][2][5])(const StepArgs<float> *);   // [log2 Ny][shape][mode]
 };
+
+// Column-pass launch shape (0 wide, 1 narrow) used for new simulations of this
+// precision and log2 Ny: a process-wide table seeded with the measured rule
+// (narrow below Ny = 2048) and updated by am_autotune / am_set_column_shape.
+int col_variant(bool fp64, int logny);
+void set_col_variant(bool fp64, int logny, int v);
 
 const BatchTable &kernels_batch_f32();
 

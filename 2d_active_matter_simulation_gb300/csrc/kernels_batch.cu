@@ -12,13 +12,13 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
     RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
-template <typename T, int LOG, int MODE>
-__global__ void __launch_bounds__(ColPass<T, LOG, MODE>::THREADS, ColPass<T, LOG, MODE>::MINB)
+template <typename T, int LOG, int MODE, int NARROW>
+__global__ void __launch_bounds__(ColPass<T, LOG, MODE, NARROW>::THREADS, ColPass<T, LOG, MODE, NARROW>::MINB)
     k_col_b(const StepArgs<T> *__restrict__ args)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const StepArgs<T> a = args[blockIdx.y];
-    ColPass<T, LOG, MODE>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+    ColPass<T, LOG, MODE, NARROW>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
 template <int LOG>
@@ -26,11 +26,16 @@ struct FillB {
     static void run(BatchTable &t)
     {
         t.row[LOG] = k_row_b<float, LOG>;
-        t.col[LOG][0] = k_col_b<float, LOG, 0>;
-        t.col[LOG][1] = k_col_b<float, LOG, 1>;
-        t.col[LOG][2] = k_col_b<float, LOG, 2>;
-        t.col[LOG][3] = k_col_b<float, LOG, 3>;
-        t.col[LOG][4] = k_col_b<float, LOG, 4>;
+        t.col[LOG][0][0] = k_col_b<float, LOG, 0, 0>;
+        t.col[LOG][0][1] = k_col_b<float, LOG, 1, 0>;
+        t.col[LOG][0][2] = k_col_b<float, LOG, 2, 0>;
+        t.col[LOG][0][3] = k_col_b<float, LOG, 3, 0>;
+        t.col[LOG][0][4] = k_col_b<float, LOG, 4, 0>;
+        t.col[LOG][1][0] = k_col_b<float, LOG, 0, 1>;
+        t.col[LOG][1][1] = k_col_b<float, LOG, 1, 1>;
+        t.col[LOG][1][2] = k_col_b<float, LOG, 2, 1>;
+        t.col[LOG][1][3] = k_col_b<float, LOG, 3, 1>;
+        t.col[LOG][1][4] = k_col_b<float, LOG, 4, 1>;
         if constexpr (LOG < BATCH_LOG_MAX) FillB<LOG + 1>::run(t);
     }
 };

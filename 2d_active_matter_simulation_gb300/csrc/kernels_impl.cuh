@@ -13,11 +13,12 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
     RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
-template <typename T, int LOG, int MODE>
-__global__ void __launch_bounds__(ColPass<T, LOG, MODE>::THREADS, ColPass<T, LOG, MODE>::MINB) k_col(StepArgs<T> a)
+template <typename T, int LOG, int MODE, int NARROW>
+__global__ void __launch_bounds__(ColPass<T, LOG, MODE, NARROW>::THREADS, ColPass<T, LOG, MODE, NARROW>::MINB)
+    k_col(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    ColPass<T, LOG, MODE>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+    ColPass<T, LOG, MODE, NARROW>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
 template <typename T, int LOG>
@@ -66,16 +67,23 @@ __global__ void k_untile(const cpx<T> *src, cpx<T> *dst, int ny, int nxh, int nt
 
 template <typename T, int LOG>
 struct Fill {
+    template <int V>
+    static void fill_col(KernelTable<T> &t)
+    {
+        t.col[LOG][V][0] = k_col<T, LOG, 0, V>;
+        t.col[LOG][V][1] = k_col<T, LOG, 1, V>;
+        t.col[LOG][V][2] = k_col<T, LOG, 2, V>;
+        t.col[LOG][V][3] = k_col<T, LOG, 3, V>;
+        t.col[LOG][V][4] = k_col<T, LOG, 4, V>;
+        using CP = ColPass<T, LOG, 1, V>;
+        t.col_shape[LOG][V] = {CP::THREADS, CP::smem_bytes(), CP::COLS};
+    }
     static void run(KernelTable<T> &t)
     {
         t.row[LOG] = k_row<T, LOG>;
         t.row_shape[LOG] = {RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::smem_bytes(), RowKernel<T, LOG>::ROWS};
-        t.col[LOG][0] = k_col<T, LOG, 0>;
-        t.col[LOG][1] = k_col<T, LOG, 1>;
-        t.col[LOG][2] = k_col<T, LOG, 2>;
-        t.col[LOG][3] = k_col<T, LOG, 3>;
-        t.col[LOG][4] = k_col<T, LOG, 4>;
-        t.col_shape[LOG] = {ColPass<T, LOG, 1>::THREADS, ColPass<T, LOG, 1>::smem_bytes(), ColPass<T, LOG, 1>::COLS};
+        fill_col<0>(t);
+        fill_col<1>(t);
         t.rowfwd[LOG] = k_rowfwd<T, LOG>;
         t.rowfwd_shape[LOG] = {RowFwd<T, LOG>::THREADS, RowFwd<T, LOG>::smem_bytes(), RowFwd<T, LOG>::ROWS};
         t.colfwd[LOG] = k_colfwd<T, LOG>;

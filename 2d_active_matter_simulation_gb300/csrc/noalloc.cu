@@ -178,12 +178,13 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
 
     const KernelTable<T> &K = table<T>();
     const LaunchShape &rs = K.row_shape[lx2];
-    const LaunchShape &cs = K.col_shape[ly2];
+    const int colv = col_variant(sizeof(T) == 8, ly2);
+    const LaunchShape &cs = K.col_shape[ly2][colv];
     if (rs.smem > 48 * 1024 &&
         cudaFuncSetAttribute((const void *)K.row[lx2], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs.smem))
         return AM_ERR_CUDA;
     for (int m = 0; m < 5; m++)
-        if (cs.smem > 48 * 1024 && cudaFuncSetAttribute((const void *)K.col[ly2][m],
+        if (cs.smem > 48 * 1024 && cudaFuncSetAttribute((const void *)K.col[ly2][colv][m],
                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cs.smem))
             return AM_ERR_CUDA;
 
@@ -196,12 +197,12 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
     const int cgrid = col_grid(cs, nt, Tile<T>::W);
     StepArgs<T> b = a;
     b.mode = 0;
-    K.col[ly2][0]<<<cgrid, cs.threads, cs.smem, st>>>(b);
+    K.col[ly2][colv][0]<<<cgrid, cs.threads, cs.smem, st>>>(b);
     for (int n = 0; n < nsteps; n++) {
         for (int stage = 1; stage <= 4; stage++) {
             K.row[lx2]<<<rgrid, rs.threads, rs.smem, st>>>(a);
             b.mode = stage;
-            K.col[ly2][stage]<<<cgrid, cs.threads, cs.smem, st>>>(b);
+            K.col[ly2][colv][stage]<<<cgrid, cs.threads, cs.smem, st>>>(b);
         }
     }
     K.untile<<<1024, 256, 0, st>>>(a.u0, (cpx<T> *)w_hat, ny, nxh, nt);

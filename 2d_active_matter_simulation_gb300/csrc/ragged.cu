@@ -67,6 +67,7 @@ struct RaggedRun {
 
 struct SizeClass {
     int lognx = 0, logny = 0;
+    int colv = 0;               // column-pass launch shape (0 wide, 1 narrow)
     std::vector<int> runs;      // run indices of this class
     std::vector<int> active;    // active runs (graph order)
     int ntp = 0;                // column tiles the passes touch (pruned or full)
@@ -177,7 +178,7 @@ am_status rebuild(am_ragged *r, const std::vector<char> &act)
         e = cudaStreamWaitEvent(c.branch, r->fork, 0);
         if (e != cudaSuccess) break;
         const LaunchShape &rs = K.row_shape[c.lognx];
-        const LaunchShape &cs = K.col_shape[c.logny];
+        const LaunchShape &cs = K.col_shape[c.logny][c.colv];
         const int ny = 1 << c.logny;
         const int nb = (int)c.active.size();
         const dim3 rgrid((ny + rs.per_block - 1) / rs.per_block, nb);
@@ -185,7 +186,7 @@ am_status rebuild(am_ragged *r, const std::vector<char> &act)
         const StepArgs<float> *args = r->dargs + c.off;
         for (int s = 1; s <= 4; s++) {
             KB.row[c.lognx]<<<rgrid, rs.threads, rs.smem, c.branch>>>(args);
-            KB.col[c.logny][s]<<<cgrid, cs.threads, cs.smem, c.branch>>>(args);
+            KB.col[c.logny][c.colv][s]<<<cgrid, cs.threads, cs.smem, c.branch>>>(args);
         }
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaEventRecord(c.joined, c.branch);
@@ -251,6 +252,7 @@ am_status am_ragged_create(const am_params *params, const long long *nsteps, int
         key[keys[c]] = (int)c;
         r->cls[c].lognx = keys[c].first;
         r->cls[c].logny = keys[c].second;
+        r->cls[c].colv = col_variant(false, keys[c].second);
     }
     size_t total = 0, stage = 0;
     for (int i = 0; i < nruns; i++) {
@@ -318,16 +320,16 @@ am_status am_ragged_create(const am_params *params, const long long *nsteps, int
     const KernelTable<float> &K = kernels_f32();
     const BatchTable &KB = kernels_batch_f32();
     for (const SizeClass &c : r->cls) {
-        const size_t rsm = K.row_shape[c.lognx].smem, csm = K.col_shape[c.logny].smem;
+        const size_t rsm = K.row_shape[c.lognx].smem, csm = K.col_shape[c.logny][c.colv].smem;
         if (rsm > 48 * 1024 &&
             cudaFuncSetAttribute((const void *)KB.row[c.lognx], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm))
             return fail(AM_ERR_CUDA);
         for (int m = 0; m < 5; m++)
-            if (csm > 48 * 1024 && cudaFuncSetAttribute((const void *)KB.col[c.logny][m],
+            if (csm > 48 * 1024 && cudaFuncSetAttribute((const void *)KB.col[c.logny][c.colv][m],
                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm))
                 return fail(AM_ERR_CUDA);
         if (csm > 48 * 1024 &&
-            cudaFuncSetAttribute((const void *)K.col[c.logny][0], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm))
+            cudaFuncSetAttribute((const void *)K.col[c.logny][c.colv][0], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm))
             return fail(AM_ERR_CUDA);
     }
     *out = r;
@@ -369,8 +371,9 @@ am_status am_ragged_set_state(am_ragged *r, int run, const void *w_hat, const do
     // start fields with the full transforms (valid however the class is pruned)
     StepArgs<float> a0 = R.a;
     set_pruning<float>(a0, false);
-    const LaunchShape &cs = K.col_shape[r->cls[R.cls].logny];
-    K.col[r->cls[R.cls].logny][0]<<<col_grid(cs, a0.ntp, Tile<float>::W), cs.threads, cs.smem, r->stream>>>(a0);
+    const SizeClass &C = r->cls[R.cls];
+    const LaunchShape &cs = K.col_shape[C.logny][C.colv];
+    K.col[C.logny][C.colv][0]<<<col_grid(cs, a0.ntp, Tile<float>::W), cs.threads, cs.smem, r->stream>>>(a0);
     RK(cudaGetLastError());
     RK(cudaStreamSynchronize(r->stream));
     R.inside = state_inside_half_mask<float>((const float *)w_hat, R.p.nx, R.p.ny);

@@ -508,18 +508,20 @@ AF_HD void cp_async_wait_all()
 
 // --------------------------------------------------------------- column pass
 // CW adjacent kx columns per group of CW * TPC threads (lane c = column in the
-// group, j = thread of that column's transform), TILES groups per CTA.
-//  * Ny >= 2048: CW = W, a whole tile per group, so every store covers whole
-//    32-byte sectors (one CTA of 512 threads per SM; FP32 at Ny = 4096 takes
-//    half a tile, 512 threads, to stay within 128 registers).
-//  * Ny <= 1024: CW = 1, one column per group: CTAs of 128 threads, up to four
-//    per SM, each synchronising only its own warps.  Stores then cover a
-//    quarter sector each, which at 2048 cost more (ncu: 4x the L2 write
-//    sectors, 36 -> 47 us) than the extra CTAs won; below it the smaller
-//    CTAs win (ragged batch of 128^2..1024^2 grids +14%).
+// group, j = thread of that column's transform), TILES groups per CTA.  Two
+// launch shapes, chosen per precision and Ny at run time (see col_variant):
+//  * wide (NARROW = 0): CW = W, a whole tile per group, so every store covers
+//    whole 32-byte sectors (FP32 at Ny = 4096 takes half a tile, 512 threads,
+//    to stay within 128 registers).  Default for Ny >= 2048.
+//  * narrow (NARROW = 1): CW = 1, one column per group: CTAs of 128 threads
+//    (FP32, Ny <= 2048), up to four per SM, each synchronising only its own
+//    warps.  Stores then cover a quarter sector each, which at 2048 cost more
+//    (ncu: 4x the L2 write sectors, 36 -> 47 us) than the extra CTAs won;
+//    below it the smaller CTAs win (ragged batch of 128^2..1024^2 grids
+//    +14%).  Default for Ny <= 1024.
 // MODE 0 starts from u0 (after set_state), MODE 1..4 is the RK stage.
 // Launch: blockDim = THREADS, gridDim = ceil(columns carried / COLS).
-template <typename T, int LOGNY, int MODE>
+template <typename T, int LOGNY, int MODE, int NARROW = (LOGNY < 11 ? 1 : 0)>
 struct ColPass {
     static constexpr int W = Tile<T>::W;
     static constexpr int LOGR = sizeof(T) == 4 ? 4 : 3;
@@ -528,7 +530,7 @@ struct ColPass {
     static constexpr int R = FFTf::R;
     static constexpr int TPC = FFTf::TPC;
     static constexpr int L = 1 << LOGNY;
-    static constexpr int CW = L < 2048 ? 1 : (W * TPC <= 512 ? W : (512 / TPC > 1 ? 512 / TPC : 1));
+    static constexpr int CW = NARROW ? 1 : (W * TPC <= 512 ? W : (512 / TPC > 1 ? 512 / TPC : 1));
     static constexpr int TILES = CW * TPC >= 128 ? 1 : 128 / (CW * TPC);   // column groups per CTA
     static constexpr int THREADS = TILES * CW * TPC;
     static constexpr int COLS = TILES * CW;                                // columns per CTA

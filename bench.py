@@ -193,6 +193,11 @@ def run_ours(args):
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
+    # column-pass launch shape chosen by the autotuner on this GPU (untimed)
+    tune = am.autotune(am.make_params(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"],
+                                      PARAMS["alpha"], PARAMS["beta"], gamma0=PARAMS["gamma0"],
+                                      gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"], precision=PRECISION),
+                       nsteps=10)
     sim = am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"], PARAMS["beta"],
                     gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"], precision=PRECISION)
     sim.set_stream(stream.cuda_stream)
@@ -295,7 +300,8 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if PRECISION == "fp32" else "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "dt": PARAMS["dt"], "dealias": PARAMS["dealias"],
                    "parallelism": "single GPU", "l2": "flushed before every timed step (256 MB write)",
-                   "timing": "CUDA events on the solver stream, one CUDA graph (8 kernels) per step"},
+                   "timing": "CUDA events on the solver stream, one CUDA graph (8 kernels) per step",
+                   "column_shape": tune[2], "autotune_ms_per_step": {"wide": tune[0], "narrow": tune[1]}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": NCU_TRAFFIC[key] if (NX == 2048 and PRECISION == "fp32" and kxc == NX // 4) else None, "kernel": dom, "algorithmic_bytes_per_launch": dom_bytes,
                      "avg_launch_ms": dom_ms, "peak_source": peak_kind,
@@ -390,6 +396,7 @@ def run_batch(args):
         lam = float(rng.uniform(2.0, 5.0))
         params.append(am.make_params(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], lam, alpha, PARAMS["beta"],
                                      gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"]))
+    tune = am.autotune(params[0], nsteps=10)   # column-pass launch shape for 512^2 on this GPU
     batch = am.Batch(params)
     w0 = [am.ic_bandlimited(NX, NY, SEED + i).astype(np.complex64) for i in range(nb)]
     for i in range(nb):
@@ -410,7 +417,8 @@ def run_batch(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"ensemble of {nb} x {NX}^2, FP32, dt={PARAMS['dt']:g}, 1/2 rule, one batch",
                    "members": nb, "timing": "host wall clock around am_batch_step (graph per step, energies "
-                                            "of all members copied back per chunk)"},
+                                            "of all members copied back per chunk)",
+                   "column_shape": tune[2]},
         "gpu_launches": 8 * args.steps, "clocks": clk,
     }
     print(json.dumps(out), flush=True)
@@ -440,6 +448,10 @@ def run_ragged(args):
     sizes = [int(2 ** rng.integers(7, 11)) for _ in range(nr)]
     steps = [int(rng.integers(1000, 5001)) for _ in range(nr)]
     params = [_drawn_params(am, rng, n) for n in sizes]
+    # column-pass launch shape per grid size, chosen by the autotuner on this GPU
+    shapes = {}
+    for n in sorted(set(sizes)):
+        shapes[f"{n}^2"] = am.autotune(params[sizes.index(n)], nsteps=10)[2]
     ics = [am.ic_bandlimited(n, n, 2000 + i).astype(np.complex64) for i, n in enumerate(sizes)]
     # warm-up: the same runs for `warmup` steps each
     warm = am.Ragged(params, [max(args.warmup, 1)] * nr)
@@ -467,6 +479,7 @@ def run_ragged(args):
         "config": {"workload": f"ragged batch: {nr} runs, grids {hist}, steps U[1000,5000] (total "
                                f"{sum(steps)} run-steps), per-run dt, 1/2 rule, FP32",
                    "runs": nr, "size_classes": classes, "seconds": dt, "grid_point_steps": gps,
+                   "column_shapes": shapes,
                    "timing": "host wall clock around am_ragged_run (one CUDA graph per step with one branch per "
                              "size class, energies of every run copied back per segment)"},
         "gpu_launches": _ragged_launches(sizes, steps), "clocks": clk,

@@ -249,6 +249,23 @@ am_status am_server_destroy(am_server *s);
 /* Device bytes a handle with these parameters holds (what admission reserves). */
 long long am_footprint_bytes(const am_params *p);
 
+/* ------------------------------------------------------ launch shapes --
+ * The column pass has two launch shapes: 0 "wide" (a whole tile of adjacent
+ * kx columns per group of threads, whole-sector stores, 512-thread CTAs) and
+ * 1 "narrow" (one column per group, 128-thread CTAs, up to four per SM).
+ * Which is faster depends on Ny and the precision; the process keeps one
+ * choice per (precision, Ny), seeded with the rule measured on GB300 (narrow
+ * below Ny = 2048), used by every handle, batch and ragged batch created
+ * afterwards.  The reference has no counterpart (cuFFT picks its own plans,
+ * ActFlow_V3-2.cu:507-508). */
+am_status am_set_column_shape(int precision, int ny, int shape);
+int am_column_shape(int precision, int ny);   /* -1 for an unsupported size */
+/* Autotune: time nsteps steps of a simulation with parameters p under each
+ * shape on the current device (a temporary handle with a seeded band-limited
+ * state), store the faster one for p's precision and Ny, and report both
+ * times in ms_per_step[2] (may be NULL). */
+am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[2]);
+
 /* Number of kernel launches one step makes (for accounting). */
 int am_launches_per_step(const am_handle *h);
 

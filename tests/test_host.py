@@ -171,3 +171,17 @@ def test_cli_error_exits(am, tmp_path):
     with open(tmp_path / "specifications.txt", "w") as f:
         f.write("dt:\n0.1\ndt_snap:\n0.01\n")
     assert subprocess.run([exe, str(tmp_path)], capture_output=True).returncode == 1
+
+
+def test_column_shape_table(am):
+    """The column-pass shape table (no GPU needed): seeded narrow below 2048,
+    settable per precision and Ny, sizes outside 8..4096 rejected."""
+    assert am.column_shape("fp32", 2048) == "wide" and am.column_shape("fp32", 1024) == "narrow"
+    assert am.column_shape("fp64", 4096) == "wide" and am.column_shape("fp64", 256) == "narrow"
+    am.set_column_shape("fp32", 512, "wide")
+    assert am.column_shape("fp32", 512) == "wide" and am.column_shape("fp64", 512) == "narrow"
+    am.set_column_shape("fp32", 512, "narrow")
+    assert am.column_shape("fp32", 512) == "narrow"
+    assert am.column_shape("fp32", 96) is None
+    with pytest.raises(am.ActflowError):
+        am.set_column_shape("fp32", 8192, "wide")

@@ -199,3 +199,23 @@ def test_server_reports_nan(am):
     srv.close()
     assert res["status"] == am.AM_ERR_NAN
     assert "NaN" in res["error"]
+
+
+def test_server_small_request_overtakes_large_one(am):
+    """Continuous batching: a small request submitted while a large one runs
+    is admitted into a free slot and, on a higher-priority stream, finishes
+    first instead of queueing behind it."""
+    big = am.make_params(2048, 2048, TWO_PI, TWO_PI, 1e-4, 3.5, -0.8, 0.01, gamma0=-0.045, gamma2=2.5e-5,
+                         dealias="half")
+    small = am.make_params(64, 64, TWO_PI, TWO_PI, 1e-3, 3.5, -0.8, 0.01, gamma0=-0.045, gamma2=2.5e-5,
+                           dealias="half")
+    srv = am.Server(max_active=4)
+    jb = srv.submit(big, 3000, seed=1, want_state=False, want_energy=False)
+    time.sleep(0.2)
+    js = srv.submit(small, 20, seed=2)
+    rs = srv.wait(js, timeout=300)
+    rb = srv.wait(jb, timeout=300)
+    srv.close()
+    assert rs["status"] == am.AM_OK and rb["status"] == am.AM_OK
+    assert rs["t_done"] < rb["t_done"]
+    assert rs["t_admit"] < rb["t_done"]

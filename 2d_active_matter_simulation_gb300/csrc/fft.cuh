@@ -173,6 +173,11 @@ struct DFT {
 //   SWZ 0: idx + idx/8          column passes (W = 4 FP32, W = 2 FP64)
 //   SWZ 1: idx ^ ((idx/16) % 16) row passes, FP32 (a permutation: no padding)
 //   SWZ 2: idx + idx/4          row passes, FP64
+//   SWZ 5: per exchange, keyed on the write stride NS of the exchange: NS = 2
+//          idx ^ ((idx/8) % 16), otherwise as SWZ 1 -- row passes, FP32:
+//          conflict-free for every exchange of the 1024-point transform
+//          (SWZ 1 alone: 1.25x the conflict-free wavefronts) and no worse at
+//          other lengths; put/get use the SWZ 1 map
 template <typename T, int W, int SWZ>
 struct XBuf {
     cpx<T> *d;
@@ -183,24 +188,29 @@ struct XBuf {
     AF_HDC static constexpr int pad(int i)
     {
         if constexpr (SWZ == 0) return i + (i >> 3);
-        else if constexpr (SWZ == 1) return i ^ ((i >> 4) & 15);
+        else if constexpr (SWZ == 1 || SWZ == 5) return i ^ ((i >> 4) & 15);
         else if constexpr (SWZ == 2) return i + (i >> 2);
         else if constexpr (SWZ == 3) return i + (i >> 4);
         else return i + (i >> 5);
     }
-    // Slot of element base + r * STRIDE for transform c.
-    template <int STRIDE>
+    // Slot of element base + r * STRIDE for transform c, in the exchange whose
+    // writes have stride NSX (SWZ 5 picks its map by it; others ignore it).
+    template <int STRIDE, int NSX = STRIDE>
     AF_HD int at(int base, int r, int c) const
     {
-        if constexpr (SWZ != 1 && (STRIDE % (1 << SH)) == 0)
+        if constexpr (SWZ == 5 && NSX == 2) {
+            const int i = base + r * STRIDE;
+            return (i ^ ((i >> 3) & 15)) * W + c;
+        } else if constexpr (SWZ != 1 && SWZ != 5 && (STRIDE % (1 << SH)) == 0) {
             return (pad(base) + r * (STRIDE + (STRIDE >> SH))) * W + c;
-        else
+        } else {
             return pad(base + r * STRIDE) * W + c;
+        }
     }
     // slots needed for L elements
     AF_HDC static constexpr int slots(int L)
     {
-        if constexpr (SWZ == 1) return (L < 16 ? 16 : L) * W;
+        if constexpr (SWZ == 1 || SWZ == 5) return (L < 16 ? 16 : L) * W;
         else return pad(L - 1) * W + W;
     }
     AF_HD void put(int idx, int c, cpx<T> v) const { d[pad(idx) * W + c] = v; }
@@ -357,7 +367,7 @@ struct BlockFFT {
             if constexpr (!FROM_REGS) {
                 const Buf &b = (SINGLE || (e & 1) == 1) ? b0 : b1;   // buffer written by exchange e-1
 #pragma unroll
-                for (int r = 0; r < R; r++) v[r] = b.d[b.template at<TPC>(j, r, c)];
+                for (int r = 0; r < R; r++) v[r] = b.d[b.template at<TPC, (P == 0 ? 1 : NS / R)>(j, r, c)];
             }
             if constexpr (NS > 1) {
                 const int k = j & (NS - 1);
@@ -384,7 +394,7 @@ struct BlockFFT {
                 const int base = (j - k) * R + k;
                 if (SINGLE && e > 0) sync();   // one buffer: earlier reads must finish
 #pragma unroll
-                for (int r = 0; r < R; r++) b.d[b.template at<NS>(base, r, c)] = v[r];
+                for (int r = 0; r < R; r++) b.d[b.template at<NS, NS>(base, r, c)] = v[r];
                 sync();
                 pass<P + 1, false, SINGLE>(v, j, c, b0, b1, tw, TWS, sync, e + 1);
             }
@@ -438,7 +448,7 @@ struct BlockFFT {
                 for (int f = 0; f < NF; f++) {
                     const Buf &b = (SINGLE || (e & 1) == 1) ? b0[f] : b1[f];   // written by exchange e-1
 #pragma unroll
-                    for (int r = 0; r < R; r++) v[f][r] = b.d[b.template at<TPC>(j, r, c)];
+                    for (int r = 0; r < R; r++) v[f][r] = b.d[b.template at<TPC, (P == 0 ? 1 : NS / R)>(j, r, c)];
                 }
             }
             if constexpr (NS > 1) {
@@ -461,7 +471,7 @@ struct BlockFFT {
                 for (int f = 0; f < NF; f++) {
                     const Buf &b = (SINGLE || (e & 1) == 0) ? b0[f] : b1[f];
 #pragma unroll
-                    for (int r = 0; r < R; r++) b.d[b.template at<NS>(base, r, c)] = v[f][r];
+                    for (int r = 0; r < R; r++) b.d[b.template at<NS, NS>(base, r, c)] = v[f][r];
                 }
                 sync();
                 pass_multi<P + 1, false, NF, SINGLE>(v, j, c, b0, b1, tw, TWS, sync, e + 1);

@@ -157,7 +157,10 @@ struct RowPass {
     // resident CTAs per SM requested from the compiler: caps registers at 128 (FP32) / 255 (FP64)
     static constexpr int MINB = sizeof(T) == 4 ? (THREADS >= 256 ? 2 : 4) : 1;
     static constexpr bool WARP_SYNC = false;
-    using Buf = XBuf<T, 1, sizeof(T) == 4 ? 1 : 2>;
+    using Buf = XBuf<T, 1, sizeof(T) == 4 ? 5 : 2>;
+    // slot of element idx in the pairing exchange of the forward transforms:
+    // FP32 unswizzled (conflict-free for its put and reversed get), FP64 padded
+    static AF_HD int pslot(int idx) { return sizeof(T) == 4 ? idx : Buf::pad(idx); }
     static constexpr int BUFS = (Buf::slots(M) + 7) / 8 * 8;   // complex slots per buffer
 
     // per row: two exchange buffers (double buffering) for each of the three
@@ -390,7 +393,7 @@ struct RowPass {
         for (int f = 0; f < 2; f++) {
             const Buf &pb = (FFTf::NEXCH & 1) ? pb1[f] : pb0[f];
 #pragma unroll
-            for (int r = 0; r < R; r++) pb.put(j + r * TPC, 0, pq[f][r]);
+            for (int r = 0; r < R; r++) pb.d[pslot(j + r * TPC)] = pq[f][r];
         }
         sync();
         const int kend = a.ntp * Tile<T>::W;   // the column pass reads kx < kend
@@ -401,7 +404,7 @@ struct RowPass {
             static_for<0, R>([&](auto rc) {
                 constexpr int r = decltype(rc)::value;
                 const int k = j + r * TPC;
-                if (active && k < kend) dst[tidx<T>(k, y, ny)] = unpack_r<r>(pq[f][r], pb.get((M - k) & (M - 1), 0), wj);
+                if (active && k < kend) dst[tidx<T>(k, y, ny)] = unpack_r<r>(pq[f][r], pb.d[pslot((M - k) & (M - 1))], wj);
             });
             if (active && j == 0 && M < kend) {   // kx = M: E(0) - O(0)
                 dst[tidx<T>(M, y, ny)] = unpack(pq[f][0], pq[f][0], mk<T>(-1, 0));

@@ -38,6 +38,18 @@ struct KernelTable {
 const KernelTable<float> &kernels_f32();
 const KernelTable<double> &kernels_f64();
 
+// Fillers of the tables, one per translation unit (ranges of log2 lengths).
+void fill_f32_3_6(KernelTable<float> &t);
+void fill_f32_7_8(KernelTable<float> &t);
+void fill_f32_9(KernelTable<float> &t);
+void fill_f32_10(KernelTable<float> &t);
+void fill_f32_11(KernelTable<float> &t);
+void fill_f32_12(KernelTable<float> &t);
+void fill_f64_3_8(KernelTable<double> &t);
+void fill_f64_9_10(KernelTable<double> &t);
+void fill_f64_11(KernelTable<double> &t);
+void fill_f64_12(KernelTable<double> &t);
+
 // Batched forms of the step kernels: one launch covers every member of an
 // ensemble (blockIdx.y = member), each member's arguments read from a device
 // array.  FP32, grids 128..1024 per axis.
@@ -56,5 +68,7 @@ int col_variant(bool fp64, int logny);
 void set_col_variant(bool fp64, int logny, int v);
 
 const BatchTable &kernels_batch_f32();
+void fill_batch_7_8(BatchTable &t);
+void fill_batch_9_10(BatchTable &t);
 
 }  // namespace af

@@ -1,53 +1,17 @@
-// Batched FP32 step kernels (blockIdx.y = ensemble member), grids 128..1024.
-#include "kernels_impl.cuh"
+// Batched FP32 step kernels for 128 and 256 and the assembled batch table.
+#include "kernels_batch_impl.cuh"
 
 namespace af {
-
-template <typename T, int LOG>
-__global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::MINB)
-    k_row_b(const StepArgs<T> *__restrict__ args)
-{
-    extern __shared__ __align__(16) unsigned char smem[];
-    const StepArgs<T> a = args[blockIdx.y];
-    RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
-}
-
-template <typename T, int LOG, int MODE, int NARROW>
-__global__ void __launch_bounds__(ColPass<T, LOG, MODE, NARROW>::THREADS, ColPass<T, LOG, MODE, NARROW>::MINB)
-    k_col_b(const StepArgs<T> *__restrict__ args)
-{
-    extern __shared__ __align__(16) unsigned char smem[];
-    const StepArgs<T> a = args[blockIdx.y];
-    ColPass<T, LOG, MODE, NARROW>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
-}
-
-template <int LOG>
-struct FillB {
-    static void run(BatchTable &t)
-    {
-        t.row[LOG] = k_row_b<float, LOG>;
-        t.col[LOG][0][0] = k_col_b<float, LOG, 0, 0>;
-        t.col[LOG][0][1] = k_col_b<float, LOG, 1, 0>;
-        t.col[LOG][0][2] = k_col_b<float, LOG, 2, 0>;
-        t.col[LOG][0][3] = k_col_b<float, LOG, 3, 0>;
-        t.col[LOG][0][4] = k_col_b<float, LOG, 4, 0>;
-        t.col[LOG][1][0] = k_col_b<float, LOG, 0, 1>;
-        t.col[LOG][1][1] = k_col_b<float, LOG, 1, 1>;
-        t.col[LOG][1][2] = k_col_b<float, LOG, 2, 1>;
-        t.col[LOG][1][3] = k_col_b<float, LOG, 3, 1>;
-        t.col[LOG][1][4] = k_col_b<float, LOG, 4, 1>;
-        if constexpr (LOG < BATCH_LOG_MAX) FillB<LOG + 1>::run(t);
-    }
-};
+void fill_batch_7_8(BatchTable &t) { FillB<7, 8>::run(t); }
 
 const BatchTable &kernels_batch_f32()
 {
     static const BatchTable t = []() {
         BatchTable b{};
-        FillB<BATCH_LOG_MIN>::run(b);
+        fill_batch_7_8(b);
+        fill_batch_9_10(b);
         return b;
     }();
     return t;
 }
-
 }  // namespace af

@@ -1,0 +1,47 @@
+// Batched FP32 step kernels (blockIdx.y = ensemble member), grids 128..1024;
+// instantiated by kernels_batch.cu (128, 256) and kernels_batch_9_10.cu
+// (512, 1024), which compile in parallel.
+#pragma once
+#include "kernels_impl.cuh"
+
+namespace af {
+
+template <typename T, int LOG>
+__global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::MINB)
+    k_row_b(const StepArgs<T> *__restrict__ args)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const StepArgs<T> a = args[blockIdx.y];
+    RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+}
+
+template <typename T, int LOG, int MODE, int NARROW>
+__global__ void __launch_bounds__(ColPass<T, LOG, MODE, NARROW>::THREADS, ColPass<T, LOG, MODE, NARROW>::MINB)
+    k_col_b(const StepArgs<T> *__restrict__ args)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const StepArgs<T> a = args[blockIdx.y];
+    ColPass<T, LOG, MODE, NARROW>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+}
+
+template <int LOG, int HI>
+struct FillB {
+    static void run(BatchTable &t)
+    {
+        t.row[LOG] = k_row_b<float, LOG>;
+        t.col[LOG][0][0] = k_col_b<float, LOG, 0, 0>;
+        t.col[LOG][0][1] = k_col_b<float, LOG, 1, 0>;
+        t.col[LOG][0][2] = k_col_b<float, LOG, 2, 0>;
+        t.col[LOG][0][3] = k_col_b<float, LOG, 3, 0>;
+        t.col[LOG][0][4] = k_col_b<float, LOG, 4, 0>;
+        t.col[LOG][1][0] = k_col_b<float, LOG, 0, 1>;
+        t.col[LOG][1][1] = k_col_b<float, LOG, 1, 1>;
+        t.col[LOG][1][2] = k_col_b<float, LOG, 2, 1>;
+        t.col[LOG][1][3] = k_col_b<float, LOG, 3, 1>;
+        t.col[LOG][1][4] = k_col_b<float, LOG, 4, 1>;
+        if constexpr (LOG < HI) FillB<LOG + 1, HI>::run(t);
+    }
+};
+
+
+}  // namespace af

@@ -1,5 +1,7 @@
-// Kernel entry points and dispatch-table construction, included once per
-// precision by kernels_f32.cu and kernels_f64.cu.
+// Kernel entry points and dispatch-table construction.  The table of a
+// precision is filled by several translation units, each instantiating a range
+// of transform lengths (kernels_f32_*.cu, kernels_f64_*.cu), so that they
+// compile in parallel; kernels_f32.cu / kernels_f64.cu assemble the tables.
 #pragma once
 #include "kernels.h"
 #include "setup_kernels.cuh"
@@ -65,7 +67,7 @@ __global__ void k_untile(const cpx<T> *src, cpx<T> *dst, int ny, int nxh, int nt
     }
 }
 
-template <typename T, int LOG>
+template <typename T, int LOG, int HI>
 struct Fill {
     template <int V>
     static void fill_col(KernelTable<T> &t)
@@ -88,18 +90,23 @@ struct Fill {
         t.rowfwd_shape[LOG] = {RowFwd<T, LOG>::THREADS, RowFwd<T, LOG>::smem_bytes(), RowFwd<T, LOG>::ROWS};
         t.colfwd[LOG] = k_colfwd<T, LOG>;
         t.colfwd_shape[LOG] = {ColFwd<T, LOG>::THREADS, ColFwd<T, LOG>::smem_bytes(), ColFwd<T, LOG>::TILES};
-        if constexpr (LOG < LOG_MAX) Fill<T, LOG + 1>::run(t);
+        if constexpr (LOG < HI) Fill<T, LOG + 1, HI>::run(t);
     }
 };
 
-template <typename T>
-KernelTable<T> make_table()
+// Entries for log2 lengths LO..HI.
+template <typename T, int LO, int HI>
+void fill_range(KernelTable<T> &t)
 {
-    KernelTable<T> t{};
-    Fill<T, LOG_MIN>::run(t);
+    Fill<T, LO, HI>::run(t);
+}
+
+// The layout-conversion kernels.
+template <typename T>
+void fill_common(KernelTable<T> &t)
+{
     t.tile = k_tile<T>;
     t.untile = k_untile<T>;
-    return t;
 }
 
 }  // namespace af

@@ -157,17 +157,23 @@ struct RowPass {
     // resident CTAs per SM requested from the compiler: caps registers at 128 (FP32) / 255 (FP64)
     static constexpr int MINB = sizeof(T) == 4 ? (THREADS >= 256 ? 2 : 4) : 1;
     static constexpr bool WARP_SYNC = false;
-    using Buf = XBuf<T, 1, sizeof(T) == 4 ? 5 : 2>;
+    // exchange slots: FP32 per-exchange XOR maps (SWZ 5), FP64 idx + idx/8
+    // (conflict-free for every exchange of the 1024-point transform with
+    // 16-byte accesses; idx + idx/4 gave 2x the wavefronts and 122 KB per CTA)
+    using Buf = XBuf<T, 1, sizeof(T) == 4 ? 5 : 0>;
     // slot of element idx in the pairing exchange of the forward transforms:
-    // FP32 unswizzled (conflict-free for its put and reversed get), FP64 padded
-    static AF_HD int pslot(int idx) { return sizeof(T) == 4 ? idx : Buf::pad(idx); }
+    // unswizzled, conflict-free for its put and its reversed get
+    static AF_HD int pslot(int idx) { return idx; }
     static constexpr int BUFS = (Buf::slots(M) + 7) / 8 * 8;   // complex slots per buffer
 
     // per row: two exchange buffers (double buffering) for each of the three
     // transforms that run in lockstep; where six do not fit in shared memory
-    // (FP64, Nx = 4096) each transform reuses one buffer for every exchange
-    // (SINGLE: one more barrier per exchange)
-    static constexpr int SINGLE = (size_t)ROWS * 6 * BUFS * sizeof(cpx<T>) > (size_t)227 * 1024 ? 1 : 0;
+    // -- for FP64 CTAs of 128 threads, where two CTAs per SM fit by registers,
+    // where they would keep a second CTA off the SM -- each transform reuses
+    // one buffer for every exchange (SINGLE: one more barrier per exchange)
+    static constexpr size_t SMEM_CAP =
+        (sizeof(T) == 8 && THREADS <= 128) ? (size_t)113 * 1024 : (size_t)227 * 1024;
+    static constexpr int SINGLE = (size_t)ROWS * 6 * BUFS * sizeof(cpx<T>) > SMEM_CAP ? 1 : 0;
     static constexpr int NBUF = SINGLE ? 3 : 6;
     static constexpr size_t smem_bytes() { return (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>); }
 

@@ -38,7 +38,7 @@ typedef enum {
     AM_ERR_IO = 4,           /* file could not be read or written */
     AM_ERR_SPEC = 5,         /* malformed specifications.txt / unknown key */
     AM_ERR_OOM = 6,          /* device allocation failed */
-    AM_ERR_UNSUPPORTED = 7,  /* request outside what this build supports */
+    AM_ERR_UNSUPPORTED = 7,  /* request outside what the library supports */
     AM_ERR_TIMEOUT = 8       /* a wait ran out before the result was ready */
 } am_status;
 

@@ -247,3 +247,51 @@ def test_gpu_pruned_state_stays_inside_ellipse(am):
     mask = np.array([[am.mask_value(nx, ny, "half", ix, iy) for ix in range(nx // 2 + 1)] for iy in range(ny)])
     assert np.abs(w[mask == 0]).max() == 0.0
     assert np.abs(w[mask == 1]).max() > 0.0
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_gpu_largest_grid_vs_oracle(am, orc, prec):
+    """The largest supported grid, 4096^2, both passes at full length, 2 steps
+    of the 1/2-rule step against the FP64 oracle."""
+    n = 4096
+    L = 2 * math.pi
+    w0 = am.ic_bandlimited(n, n, seed=5, kmin=1, kmax=8, rms=0.5)
+    mean0 = (0.01 * n * n, -0.02 * n * n)
+    sim = am.Solver(n, n, L, L, 1e-4, 3.5, -0.8, 0.01, gamma0=-0.045, gamma2=2.5e-5, dealias="half", precision=prec)
+    sim.set_state(w0 if prec == "fp64" else w0.astype(np.complex64), mean0)
+    e = sim.step(2)
+    w, m = sim.get_state()
+    sim.close()
+    p = orc.make_params(n, n, L, L, 1e-4, 3.5, -0.8, 0.01, -0.045, 2.5e-5, dealias="half")
+    wo, mo, eo = orc.run(p, w0, mean0, 2, "f64")
+    tol = 1e-10 if prec == "fp64" else 2e-5
+    assert rel(w, wo) < tol
+    assert np.abs(e - eo).max() <= tol * np.abs(eo).max()
+    assert np.abs(m - mo).max() <= tol * np.abs(mo).max()
+
+
+def test_gpu_zero_steps_leave_the_state(am):
+    """nsteps = 0 through every entry point: nothing advances, nothing fails."""
+    n = 64
+    w0 = am.ic_bandlimited(n, n, seed=3, rms=0.5).astype(np.complex64)
+    sim = am.Solver(n, n, 2 * math.pi, 2 * math.pi, 1e-3, 3.5, -0.8, 0.01, dealias="half")
+    sim.set_state(w0, (1.0, 2.0))
+    assert len(sim.step(0)) == 0
+    w, m = sim.get_state()
+    sim.close()
+    assert np.array_equal(w, w0) and np.array_equal(m, [1.0, 2.0])
+    p = am.make_params(128, 128, 2 * math.pi, 2 * math.pi, 1e-3, 3.5, -0.8, 0.01, dealias="half")
+    r = am.Ragged([p, p], [0, 3])
+    wr = am.ic_bandlimited(128, 128, seed=4, rms=0.5).astype(np.complex64)
+    r.set_state(0, wr)
+    r.set_state(1, wr)
+    energies, gps = r.run()
+    assert gps == 3 * 128 * 128 and len(energies[0]) == 0 and len(energies[1]) == 3
+    assert np.array_equal(r.get_state(0)[0], wr) and not np.array_equal(r.get_state(1)[0], wr)
+    r.close()
+    srv = am.Server()
+    res = srv.wait(srv.submit(p, 0, seed=9), timeout=60)
+    srv.close()
+    assert res["status"] == am.AM_OK and res["steps_done"] == 0
+    w9 = am.ic_bandlimited(128, 128, 9, 1.0, 8.0, 0.01).astype(np.complex64)
+    assert np.array_equal(res["state"], w9)

@@ -339,11 +339,15 @@ def run_accuracy(args):
     w0 = am.ic_bandlimited(NX, NY, SEED)
     res = {}
     runs = {}
-    for prec in ("fp32", "fp64"):
+    # "twin": FP64 from the same field perturbed by one part in 1e12 -- the
+    # spread of the chaotic flow itself, against which the FP32 vs FP64
+    # long-horizon differences are read
+    w0_twin = w0 * (1.0 + 1e-12)
+    for prec in ("fp32", "fp64", "twin"):
         sim = am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"],
                         PARAMS["beta"], gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"],
-                        dealias=PARAMS["dealias"], precision=prec)
-        sim.set_state(w0 if prec == "fp64" else w0.astype(np.complex64))
+                        dealias=PARAMS["dealias"], precision="fp32" if prec == "fp32" else "fp64")
+        sim.set_state(w0 if prec == "fp64" else w0_twin if prec == "twin" else w0.astype(np.complex64))
         t0 = time.perf_counter()
         e = [sim.step(200)]
         w200, _ = sim.get_state()
@@ -374,6 +378,13 @@ def run_accuracy(args):
         sa, sb = a["spec"][: kmax + 1], b["spec"][: kmax + 1]
         res["spectrum_l1_rel_diff"] = float(np.sum(np.abs(sa - sb)) / np.sum(sb))
         res["spectrum_snapshots"] = (n_total - n_total // 2) // 200
+    t = runs["twin"]
+    res["twin_w_rel_l2_200"] = float(np.linalg.norm(t["w200"] - b["w200"]) / np.linalg.norm(b["w200"]))
+    res["twin_mean_energy_rel_diff"] = abs(float(np.mean(t["energy"][half:])) / res["mean_energy_fp64"] - 1)
+    if t["spec"] is not None and b["spec"] is not None:
+        st, s64 = t["spec"][: NX // 4 + 1], b["spec"][: NX // 4 + 1]
+        res["twin_spectrum_l1_rel_diff"] = float(np.sum(np.abs(st - s64)) / np.sum(s64))
+    res["energy_fp64_first_last"] = [float(b["energy"][0]), float(b["energy"][half]), float(b["energy"][-1])]
     res["seconds_fp32"] = a["seconds"]
     res["seconds_fp64"] = b["seconds"]
     res["gps_fp64"] = NX * NY * n_total / b["seconds"]

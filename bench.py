@@ -31,6 +31,52 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+
+# ---- replicas (--gpus N > 1 under torchrun): one independent simulation per
+# GPU, no data exchange (the step has none); the ranks meet only at the
+# barriers around the timed region and in the max of their times, over gloo.
+def replica_device(local_rank, visible):
+    """CUDA_VISIBLE_DEVICES for a rank: its own entry of the visible list (or
+    its index when none is set).  The solver library carries its own CUDA
+    runtime, so the device is chosen by visibility before anything loads."""
+    ids = [d.strip() for d in visible.split(",") if d.strip()] if visible else []
+    return ids[local_rank] if local_rank < len(ids) else str(local_rank)
+
+
+def world():
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
+
+
+def replica_setup():
+    """Bind this rank to its GPU and join the host-side process group."""
+    n, _ = world()
+    if n <= 1:
+        return
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    os.environ["CUDA_VISIBLE_DEVICES"] = replica_device(lr, os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group("gloo")
+
+
+def replica_barrier():
+    n, _ = world()
+    if n > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def replica_max(x):
+    """Largest value of x over the ranks (x itself on one GPU)."""
+    n, _ = world()
+    if n <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
 NX = NY = 2048
 PARAMS = dict(lx=2 * math.pi, ly=2 * math.pi, dt=1e-4, lam=3.5, alpha=-0.8, beta=0.01,
               gamma0=-0.045, gamma2=2.5e-5, dealias="half")
@@ -213,6 +259,7 @@ def run_ours(args):
     clocks = ClockSampler()
     clocks.start()
     torch.cuda.synchronize()
+    replica_barrier()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with torch.cuda.stream(stream):
         for i in range(args.steps):
@@ -225,8 +272,10 @@ def run_ours(args):
     ms = [a.elapsed_time(b) for a, b in ev]
     clk = clocks.stop()
     sim.sync()
-    total_ms = sum(ms)
-    value = NX * NY * args.steps / (total_ms / 1e3)
+    replica_barrier()
+    nrep, rank = world()
+    total_ms = replica_max(sum(ms))
+    value = nrep * NX * NY * args.steps / (total_ms / 1e3)
 
     # ---- per-kernel times for the roofline (same stream, L2 flushed per step)
     row = np.zeros(4)
@@ -274,15 +323,15 @@ def run_ours(args):
     am._check(am.lib.am_step(sim.h, args.steps, eo.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                              ctypes.byref(nan_at)), sim.h, "step")
     am._check(am.lib.am_get_state(sim.h, wo.ctypes.data, am._dptr(m)), sim.h, "get_state")
-    e2e_s = time.perf_counter() - t0
-    e2e_value = NX * NY * args.steps / e2e_s
+    e2e_s = replica_max(time.perf_counter() - t0)
+    e2e_value = nrep * NX * NY * args.steps / e2e_s
     state_bytes = H * s
     launches = sim.launches_per_step * args.steps
     sim.close()
 
     # ---- CPU baseline: the oracle on the host cores, bounded sample
     cpu = None
-    if not args.no_cpu and PRECISION == "fp32":
+    if not args.no_cpu and PRECISION == "fp32" and nrep == 1:
         n_cpu = 0
         t_cpu = 0.0
         cores = 1
@@ -295,11 +344,13 @@ def run_ours(args):
                          f"OpenMP, FP32), {t_cpu:.1f} s"}
 
     out = {
-        "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s", "n_gpus": 1,
+        "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s", "n_gpus": nrep,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if PRECISION == "fp32" else "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "dt": PARAMS["dt"], "dealias": PARAMS["dealias"],
-                   "parallelism": "single GPU", "l2": "flushed before every timed step (256 MB write)",
+                   "parallelism": "single GPU" if world()[0] == 1 else
+                   f"{world()[0]} independent replicas (one simulation per GPU, no exchange)",
+                   "l2": "flushed before every timed step (256 MB write)",
                    "timing": "CUDA events on the solver stream, one CUDA graph (8 kernels) per step",
                    "column_shape": tune[2], "autotune_ms_per_step": {"wide": tune[0], "narrow": tune[1]}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -317,7 +368,8 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk,
     }
-    print(json.dumps(out), flush=True)
+    if world()[1] == 0:
+        print(json.dumps(out), flush=True)
 
 
 def run_accuracy(args):
@@ -602,10 +654,14 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="config 4: arrival window")
     ap.add_argument("--serve-step-scale", type=float, default=0.05, help="config 4: step-count scale")
     args = ap.parse_args()
+    if args.impl == "ours":
+        replica_setup()   # before torch or the solver touch a GPU
     apply_preset(args.config, args.precision)
     if args.accuracy:
         run_accuracy(args)
         return
+    if args.config in (2, 3, 4) and world()[1] != 0:
+        return   # the ensemble, ragged and serving workloads run on one GPU (rank 0)
     if args.config == 2 and args.impl == "ours":
         run_batch(args)
         return
@@ -614,11 +670,6 @@ def main():
         return
     if args.config == 4 and args.impl == "ours":
         run_serving(args)
-        return
-    if args.gpus != 1:
-        if int(os.environ.get("RANK", "0")) == 0:
-            print(json.dumps({"error": "this solver runs one simulation per GPU; replicas are independent, "
-                                       "run with --gpus 1"}))
         return
     if args.impl == "reference":
         run_reference(args)

@@ -1,0 +1,53 @@
+"""bench.py --gpus N > 1: independent replicas, one simulation per GPU.  The
+ranks share no data; the host-side helpers (device selection, barrier, max of
+the timed region over ranks) are exercised here with two gloo ranks on CPU."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_replica_device_mapping():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.replica_device(0, "") == "0" and bench.replica_device(3, "") == "3"
+    assert bench.replica_device(1, "4,5,6") == "5"
+    assert bench.replica_device(0, " 7 , 2") == "7"
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), WORLD_SIZE="2", RANK=str(rank),
+                      LOCAL_RANK=str(rank), CUDA_VISIBLE_DEVICES="")
+    sys.path.insert(0, ROOT)
+    import bench
+    bench.replica_setup()
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == str(rank)
+    bench.replica_barrier()
+    m = bench.replica_max(10.0 + rank)
+    out.put((rank, m, bench.world()))
+    import torch.distributed as dist
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_take_the_max():
+    mp = pytest.importorskip("torch.multiprocessing")
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    ps = [ctx.Process(target=_rank, args=(r, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert res == [(0, 11.0, (2, 0)), (1, 11.0, (2, 1))]

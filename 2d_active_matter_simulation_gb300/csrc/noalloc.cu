@@ -31,7 +31,10 @@ constexpr size_t kScratchBytes = 8u << 20;   // 8 MiB per device
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 // Device address of g_scratch per device, looked up once per device with that
-// device current (the symbol name is only a host-side stand-in).
+// device current (the symbol name is only a host-side stand-in).  The address
+// belongs to the device's context: cudaDeviceReset destroys that context and
+// the array with it, so the cached address must not be used after a reset
+// (the entry point's documentation says so).
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned char *g_ptr[kMaxDevices];
@@ -223,6 +226,9 @@ extern "C" am_status am_step_noalloc(const am_params *p, void *w_hat, double *me
     if (p->precision != AM_FP32 && p->precision != AM_FP64) return AM_ERR_ARG;
     if (p->dealias < 0 || p->dealias > 2 || (p->form != AM_FORM_REFERENCE && p->form != AM_FORM_GENERAL))
         return AM_ERR_ARG;
+    // the parameter checks of am_create: a non-positive box length makes the
+    // wavenumber tables infinite and the state NaN
+    if (!(p->lx > 0) || !(p->ly > 0) || !std::isfinite(p->dt)) return AM_ERR_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     return p->precision == AM_FP64 ? run<double>(*p, w_hat, mean, nsteps, energy, st)
                                    : run<float>(*p, w_hat, mean, nsteps, energy, st);

@@ -36,11 +36,19 @@ sys.path.insert(0, ROOT)
 # GPU, no data exchange (the step has none); the ranks meet only at the
 # barriers around the timed region and in the max of their times, over gloo.
 def replica_device(local_rank, visible):
-    """CUDA_VISIBLE_DEVICES for a rank: its own entry of the visible list (or
-    its index when none is set).  The solver library carries its own CUDA
-    runtime, so the device is chosen by visibility before anything loads."""
-    ids = [d.strip() for d in visible.split(",") if d.strip()] if visible else []
-    return ids[local_rank] if local_rank < len(ids) else str(local_rank)
+    """CUDA_VISIBLE_DEVICES for a rank: its own entry of the visible list, or
+    its index when the variable is unset (visible is None).  A list that is set
+    but has no entry for this rank (including an empty one, which hides every
+    GPU) is an error: falling back to the rank's index would select a GPU
+    outside the devices this job was given.  The solver library carries its own
+    CUDA runtime, so the device is chosen by visibility before anything loads."""
+    if visible is None:
+        return str(local_rank)
+    ids = [d.strip() for d in visible.split(",") if d.strip()]
+    if local_rank >= len(ids):
+        raise RuntimeError(f"local rank {local_rank} has no device in CUDA_VISIBLE_DEVICES={visible!r} "
+                           f"({len(ids)} visible)")
+    return ids[local_rank]
 
 
 def world():
@@ -53,7 +61,7 @@ def replica_setup():
     if n <= 1:
         return
     lr = int(os.environ.get("LOCAL_RANK", "0"))
-    os.environ["CUDA_VISIBLE_DEVICES"] = replica_device(lr, os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    os.environ["CUDA_VISIBLE_DEVICES"] = replica_device(lr, os.environ.get("CUDA_VISIBLE_DEVICES"))
     import torch.distributed as dist
     if not dist.is_initialized():
         dist.init_process_group("gloo")

@@ -128,13 +128,21 @@ am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double co
  * mean velocity, read and overwritten), energy[nsteps] (energy of the state
  * entering each step) or NULL.  Every intermediate buffer comes from one
  * library-owned device array of 8 MiB (held by every GPU that loads the
- * library until the process exits): grids whose scratch does not fit -- larger
- * than 512^2 in FP32 or 512x256 in FP64 -- are refused with AM_ERR_UNSUPPORTED.
+ * library until the process exits).  A call needs 7 fields of
+ * ceil((Nx/2+1)/W)*W*Ny complex values (W = 4 in FP32, 2 in FP64; each field
+ * rounded up to 256 bytes) plus at most 24*(Nx+Ny) + 56*Ny bytes of tables and
+ * sums; grids that do not fit are refused with AM_ERR_UNSUPPORTED before
+ * anything is touched.  In practice FP32 takes Nx*Ny <= 2^18 (512^2, 1024x256,
+ * 256x1024, ...) except 64x4096, FP64 Nx*Ny <= 2^17 except 32x4096.  The same
+ * parameter checks as am_create apply (AM_ERR_ARG).
  * The first call on a device looks up that array's device address (do it before
- * any stream capture).  The work is enqueued on `stream` (a cudaStream_t, NULL =
- * default stream) and the call returns without waiting; it runs the full
- * transforms and reports no NaN (check mean or the energies).  Calls share the
- * array: calls that overlap on the GPU race and must be serialised. */
+ * any stream capture); the address is kept for the process, so a device that
+ * has been through cudaDeviceReset must not be used with this entry point again
+ * (the reset destroyed the array).  The work is enqueued on `stream` (a
+ * cudaStream_t, NULL = default stream) and the call returns without waiting; it
+ * runs the full transforms and reports no NaN (check mean or the energies).
+ * Calls share the array: calls that overlap on the GPU race and must be
+ * serialised. */
 am_status am_step_noalloc(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy, void *stream);
 
 /* ------------------------------------------------------------ ensembles --

@@ -13,9 +13,18 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def test_replica_device_mapping():
     sys.path.insert(0, ROOT)
     import bench
-    assert bench.replica_device(0, "") == "0" and bench.replica_device(3, "") == "3"
+    # unset: the rank's own index
+    assert bench.replica_device(0, None) == "0" and bench.replica_device(3, None) == "3"
     assert bench.replica_device(1, "4,5,6") == "5"
     assert bench.replica_device(0, " 7 , 2") == "7"
+    # a list without an entry for the rank must not fall back to a GPU outside it
+    with pytest.raises(RuntimeError, match="no device"):
+        bench.replica_device(2, "4,5")
+    with pytest.raises(RuntimeError, match="no device"):
+        bench.replica_device(3, "4,5")
+    # set but empty: every GPU is hidden, so no rank may pick one
+    with pytest.raises(RuntimeError, match="no device"):
+        bench.replica_device(0, "")
 
 
 def _free_port():
@@ -26,11 +35,11 @@ def _free_port():
 
 def _rank(rank, port, out):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), WORLD_SIZE="2", RANK=str(rank),
-                      LOCAL_RANK=str(rank), CUDA_VISIBLE_DEVICES="")
+                      LOCAL_RANK=str(rank), CUDA_VISIBLE_DEVICES="3,1")
     sys.path.insert(0, ROOT)
     import bench
     bench.replica_setup()
-    assert os.environ["CUDA_VISIBLE_DEVICES"] == str(rank)
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == ("3", "1")[rank]
     bench.replica_barrier()
     m = bench.replica_max(10.0 + rank)
     out.put((rank, m, bench.world()))

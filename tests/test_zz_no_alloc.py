@@ -28,11 +28,12 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("prec,nx,ny", [("fp32", 256, 128), ("fp64", 256, 128),
+                                        # the largest FP32 size class, non-square (Nx*Ny = 2^18)
+                                        ("fp32", 1024, 256)])
 @pytest.mark.parametrize("dealias", ["reference", "half"])
-def test_noalloc_matches_handle_path_two_calls(am, prec, dealias):
+def test_noalloc_matches_handle_path_two_calls(am, prec, nx, ny, dealias):
     torch = pytest.importorskip("torch")
-    nx, ny = 256, 128
     lx, ly, dt, lam, alpha, beta = 40.0, 20.0, 0.004, 7.0, -0.8, 0.01
     w0 = am.ic_bandlimited(nx, ny, seed=21, kmax=12.0, rms=1.0)
     mean0 = np.array([0.2 * nx * ny, -0.1 * nx * ny])
@@ -92,3 +93,21 @@ def test_noalloc_energy_optional_and_size_limit(am):
     assert _call(am, big, w_dev, m_dev, 1, None, stream) == am.AM_ERR_UNSUPPORTED
     torch.cuda.synchronize()
     assert torch.equal(before, w_dev)
+
+
+def test_noalloc_rejects_bad_parameters(am):
+    """The checks of am_create: a non-positive box length or a non-finite dt is
+    refused before anything is enqueued, and the caller's buffers stay as they were."""
+    torch = pytest.importorskip("torch")
+    nx = ny = 64
+    w0 = am.ic_bandlimited(nx, ny, seed=4, kmax=6.0, rms=1.0).astype(np.complex64)
+    w_dev = torch.from_numpy(w0).cuda()
+    m_dev = torch.tensor([1.0, 2.0], dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    for lx, ly, dt in ((0.0, 10.0, 0.005), (10.0, -1.0, 0.005), (10.0, 10.0, float("nan")),
+                       (10.0, 10.0, float("inf"))):
+        params = am.Params(nx, ny, lx, ly, dt, 7.0, -0.8, 0.01, 0.0, 0.0, am.FORM_REFERENCE, 0, am.FP32)
+        before_w, before_m = w_dev.clone(), m_dev.clone()
+        assert _call(am, params, w_dev, m_dev, 2, None, stream) == am.AM_ERR_ARG
+        torch.cuda.synchronize()
+        assert torch.equal(before_w, w_dev) and torch.equal(before_m, m_dev)

@@ -26,6 +26,8 @@ CLI_PATH = os.path.join(HERE, "lib", "actflow")
 ORDER = {"arrival": 0, "shortest": 1}
 FP32, FP64 = 0, 1
 DEALIAS = {"reference": 0, "half": 1, "none": 2}
+# integrating factors: per value in the state precision (lin_func) or precomputed in double
+IF_FACTORS = {"auto": 0, "float": 1, "double": 2}
 FORM_REFERENCE, FORM_GENERAL = 0, 1
 
 
@@ -36,7 +38,7 @@ class Params(ctypes.Structure):
         ("lam", ctypes.c_double), ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
         ("gamma0", ctypes.c_double), ("gamma2", ctypes.c_double),
         ("form", ctypes.c_int), ("dealias", ctypes.c_int), ("precision", ctypes.c_int),
-        ("reserved", ctypes.c_int * 5),
+        ("if_factors", ctypes.c_int), ("reserved", ctypes.c_int * 4),
     ]
 
 
@@ -185,13 +187,14 @@ class Solver:
     """One simulation on the GPU (an am_handle)."""
 
     def __init__(self, nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None,
-                 dealias="reference", precision="fp32"):
+                 dealias="reference", precision="fp32", if_factors="auto"):
         form = FORM_REFERENCE if gamma0 is None else FORM_GENERAL
         self.precision = FP64 if precision in ("fp64", FP64) else FP32
         self.params = Params(nx, ny, lx, ly, dt, lam, alpha, beta,
                              0.0 if gamma0 is None else gamma0, 0.0 if gamma2 is None else gamma2,
                              form, DEALIAS[dealias] if isinstance(dealias, str) else int(dealias),
-                             self.precision)
+                             self.precision, IF_FACTORS[if_factors] if isinstance(if_factors, str)
+                             else int(if_factors))
         self.nx, self.ny = nx, ny
         self.h = ctypes.c_void_p()
         _check(lib.am_create(ctypes.byref(self.params), ctypes.byref(self.h)), None, "am_create")
@@ -456,12 +459,13 @@ def autotune(params, nsteps=20):
 
 
 def make_params(nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None, dealias="reference",
-                precision="fp32"):
+                precision="fp32", if_factors="auto"):
     form = FORM_REFERENCE if gamma0 is None else FORM_GENERAL
     return Params(nx, ny, lx, ly, dt, lam, alpha, beta, 0.0 if gamma0 is None else gamma0,
                   0.0 if gamma2 is None else gamma2, form,
                   DEALIAS[dealias] if isinstance(dealias, str) else int(dealias),
-                  FP64 if precision in ("fp64", FP64) else FP32)
+                  FP64 if precision in ("fp64", FP64) else FP32,
+                  IF_FACTORS[if_factors] if isinstance(if_factors, str) else int(if_factors))
 
 
 def mask_value(nx, ny, dealias, ix, iy):

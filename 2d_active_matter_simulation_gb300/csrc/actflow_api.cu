@@ -53,6 +53,7 @@ struct am_handle {
     // device memory
     void *u0 = nullptr, *acc = nullptr, *fa = nullptr, *fx = nullptr, *fy = nullptr, *P = nullptr, *Q = nullptr;
     void *stage = nullptr, *twx = nullptr, *twy = nullptr, *kxt = nullptr, *kyt = nullptr;
+    void *lin = nullptr;           // integrating-factor table (AM_IF_DOUBLE), one field
     double *rowp = nullptr, *energy = nullptr;
     Scalars *sc = nullptr;
     long long bytes = 0;
@@ -112,6 +113,10 @@ static am_status alloc_and_tables(am_handle *h)
     }
     CK(h, cudaMallocAsync(&h->stage, stage, h->stream));
     h->bytes += stage;
+    if (use_if_table(p)) {
+        CK(h, cudaMallocAsync(&h->lin, field, h->stream));
+        h->bytes += field;
+    }
     CK(h, cudaMallocAsync(&h->twx, nx * sizeof(cpx<T>), h->stream));
     CK(h, cudaMallocAsync(&h->twy, ny * sizeof(cpx<T>), h->stream));
     CK(h, cudaMallocAsync(&h->kxt, h->nt * W * sizeof(T), h->stream));
@@ -145,6 +150,11 @@ static am_status alloc_and_tables(am_handle *h)
     set_side<T>(a, h->rowp, ny);
     a.sc = h->sc;
     a.energy = h->energy;
+    if (h->lin) {
+        table<T>().lintab<<<1024, 256, 0, h->stream>>>((cpx<T> *)h->lin, nx, ny, h->nt, lin_coef(p));
+        CK(h, cudaGetLastError());
+        a.lintab = (const cpx<T> *)h->lin;
+    }
 
     // Opt in to large dynamic shared memory where needed.
     const KernelTable<T> &K = table<T>();
@@ -435,6 +445,7 @@ am_status am_create(const am_params *p, am_handle **out)
     if (p->dealias < 0 || p->dealias > 2 || (p->form != AM_FORM_REFERENCE && p->form != AM_FORM_GENERAL))
         return AM_ERR_ARG;
     if (!(p->lx > 0) || !(p->ly > 0) || !std::isfinite(p->dt)) return AM_ERR_ARG;
+    if (p->if_factors < AM_IF_AUTO || p->if_factors > AM_IF_DOUBLE) return AM_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return AM_ERR_CUDA;
     am_handle *h = new (std::nothrow) am_handle();
@@ -466,7 +477,7 @@ am_status am_destroy(am_handle *h)
     // Stream-ordered frees: the memory returns to the pool once the handle's
     // own work is done, without waiting for other streams of the device.
     void *ptrs[] = {h->u0, h->acc, h->fa, h->fx, h->fy, h->P, h->Q, h->stage, h->twx, h->twy,
-                    h->kxt, h->kyt, h->rowp, h->energy, h->sc};
+                    h->kxt, h->kyt, h->lin, h->rowp, h->energy, h->sc};
     for (void *q : ptrs)
         if (q) cudaFreeAsync(q, h->stream);
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -550,28 +561,52 @@ am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double co
 {
     if (!h || nsteps < 0 || !row_ms || !col_ms) return AM_ERR_ARG;
     if (!h->state_loaded) return AM_ERR_ARG;
-    cudaEvent_t ev[9];
+    // One step captured as a graph with a timing event before and after each
+    // of the 8 kernels (external event-record nodes), so the kernels run as in
+    // the production graph: back to back, no host work between them.
+    cudaEvent_t ev[9] = {};
     for (auto &e : ev) CK(h, cudaEventCreate(&e));
     am_status st = AM_OK;
-    for (int m = 0; m < nsteps && !st; m++) {
-        CK(h, cudaEventRecord(ev[0], h->stream));
-        for (int s = 1; s <= 4 && !st; s++) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (ce != cudaSuccess) st = cuda_fail(h, ce, "cudaStreamBeginCapture");
+    if (!st) {
+        ce = cudaEventRecordWithFlags(ev[0], h->stream, cudaEventRecordExternal);
+        for (int s = 1; s <= 4 && !st && ce == cudaSuccess; s++) {
             st = h->fp64 ? launch_row<double>(h) : launch_row<float>(h);
-            if (!st) CK(h, cudaEventRecord(ev[2 * s - 1], h->stream));
-            if (!st) st = h->fp64 ? launch_col<double>(h, s) : launch_col<float>(h, s);
-            if (!st) CK(h, cudaEventRecord(ev[2 * s], h->stream));
+            if (!st) ce = cudaEventRecordWithFlags(ev[2 * s - 1], h->stream, cudaEventRecordExternal);
+            if (!st && ce == cudaSuccess) st = h->fp64 ? launch_col<double>(h, s) : launch_col<float>(h, s);
+            if (!st && ce == cudaSuccess) ce = cudaEventRecordWithFlags(ev[2 * s], h->stream, cudaEventRecordExternal);
         }
-        if (st) break;
-        CK(h, cudaEventSynchronize(ev[8]));
-        for (int s = 1; s <= 4; s++) {
+        cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
+        if (!st && ce != cudaSuccess) st = cuda_fail(h, ce, "cudaEventRecordWithFlags");
+        if (!st && ee != cudaSuccess) st = cuda_fail(h, ee, "cudaStreamEndCapture");
+    }
+    if (!st) {
+        ce = cudaGraphInstantiate(&ge, g, 0);
+        if (ce != cudaSuccess) st = cuda_fail(h, ce, "cudaGraphInstantiate");
+    }
+    for (int m = 0; m < nsteps && !st; m++) {
+        ce = cudaGraphLaunch(ge, h->stream);
+        if (ce == cudaSuccess) ce = cudaEventSynchronize(ev[8]);
+        if (ce != cudaSuccess) {
+            st = cuda_fail(h, ce, "profiled step");
+            break;
+        }
+        for (int s = 1; s <= 4 && !st; s++) {
             float a = 0, b = 0;
-            CK(h, cudaEventElapsedTime(&a, ev[2 * s - 2], ev[2 * s - 1]));
-            CK(h, cudaEventElapsedTime(&b, ev[2 * s - 1], ev[2 * s]));
+            ce = cudaEventElapsedTime(&a, ev[2 * s - 2], ev[2 * s - 1]);
+            if (ce == cudaSuccess) ce = cudaEventElapsedTime(&b, ev[2 * s - 1], ev[2 * s]);
+            if (ce != cudaSuccess) st = cuda_fail(h, ce, "cudaEventElapsedTime");
             row_ms[s - 1] += a;
             col_ms[s - 1] += b;
         }
     }
-    for (auto &e : ev) cudaEventDestroy(e);
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    for (auto &e : ev)
+        if (e) cudaEventDestroy(e);
     return st;
 }
 
@@ -650,7 +685,7 @@ long long am_footprint_bytes(const am_params *p)
     const int W = f64 ? Tile<double>::W : Tile<float>::W;
     const int nxh = p->nx / 2 + 1, nt = (nxh + W - 1) / W;
     const size_t field = (size_t)nt * W * p->ny * cs;
-    return (long long)(7 * field + (size_t)p->ny * nxh * cs + (size_t)(p->nx + p->ny) * cs +
+    return (long long)((use_if_table(*p) ? 8 : 7) * field + (size_t)p->ny * nxh * cs + (size_t)(p->nx + p->ny) * cs +
                        (size_t)nt * W * rs + (size_t)p->ny * rs + side_bytes(p->ny) + ECAP * sizeof(double) +
                        sizeof(Scalars));
 }

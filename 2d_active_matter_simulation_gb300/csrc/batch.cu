@@ -36,6 +36,7 @@ struct am_batch {
     cudaStream_t stream = nullptr;
     size_t field_elems = 0;
     cpx<float> *fields = nullptr;   // [B][7][field]
+    cpx<float> *lin = nullptr;      // [B][field] integrating-factor tables (members with AM_IF_DOUBLE)
     cpx<float> *stage = nullptr;
     cpx<float> *twx = nullptr, *twy = nullptr;
     float *kxt = nullptr, *kyt = nullptr;
@@ -142,6 +143,11 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
     }
     if (p0.dealias < 0 || p0.dealias > 2 || (p0.form != AM_FORM_REFERENCE && p0.form != AM_FORM_GENERAL))
         return AM_ERR_ARG;
+    bool any_lin = false;
+    for (int i = 0; i < nmembers; i++) {
+        if (params[i].if_factors < AM_IF_AUTO || params[i].if_factors > AM_IF_DOUBLE) return AM_ERR_ARG;
+        any_lin = any_lin || use_if_table(params[i]);
+    }
     am_batch *b = new (std::nothrow) am_batch();
     if (!b) return AM_ERR_OOM;
     b->p.assign(params, params + nmembers);
@@ -168,6 +174,7 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
     const size_t B = (size_t)nmembers;
     if (cudaMalloc(&b->fields, B * 7 * fbytes) != cudaSuccess) return fail(AM_ERR_OOM);
     if (cudaMemsetAsync(b->fields, 0, B * 7 * fbytes, b->stream) != cudaSuccess) return fail(AM_ERR_CUDA);
+    if (any_lin && cudaMalloc(&b->lin, B * fbytes) != cudaSuccess) return fail(AM_ERR_OOM);
     if (cudaMalloc(&b->stage, (size_t)b->ny * b->nxh * sizeof(cpx<float>)) != cudaSuccess ||
         cudaMalloc(&b->twx, b->nx * sizeof(cpx<float>)) != cudaSuccess ||
         cudaMalloc(&b->twy, b->ny * sizeof(cpx<float>)) != cudaSuccess ||
@@ -202,6 +209,12 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
         set_side<float>(a, reinterpret_cast<unsigned char *>(b->rowp) + i * side_bytes(b->ny), b->ny);
         a.sc = b->sc + i;
         a.energy = b->energy + (size_t)i * ECAP_B;
+        if (use_if_table(b->p[i])) {
+            cpx<float> *lin = b->lin + (size_t)i * b->field_elems;
+            kernels_f32().lintab<<<1024, 256, 0, b->stream>>>(lin, b->nx, b->ny, b->nt, lin_coef(b->p[i]));
+            if (cudaGetLastError() != cudaSuccess) return fail(AM_ERR_CUDA);
+            a.lintab = lin;
+        }
     }
     // Large shared-memory opt-in for the batched kernels (same sizes as the single ones).
     const KernelTable<float> &K = kernels_f32();
@@ -227,7 +240,8 @@ am_status am_batch_destroy(am_batch *b)
     if (!b) return AM_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    void *ptrs[] = {b->fields, b->stage, b->twx, b->twy, b->kxt, b->kyt, b->rowp, b->energy, b->sc, b->dargs};
+    void *ptrs[] = {b->fields, b->lin, b->stage, b->twx, b->twy, b->kxt, b->kyt, b->rowp, b->energy, b->sc,
+                    b->dargs};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (b->stream) cudaStreamDestroy(b->stream);

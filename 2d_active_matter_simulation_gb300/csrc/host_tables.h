@@ -7,7 +7,7 @@
 #include <vector>
 
 #include "actflow.h"
-#include "step_kernels.cuh"
+#include "kernels.h"
 
 namespace af {
 
@@ -98,6 +98,32 @@ void host_setup(const am_params &p, HostTables<T> &t, StepArgs<T> &a, int ecap)
     set_mean_flow_coeffs<T>(a);
     a.inv_2n3 = 1.0 / (2.0 * nd * nd * nd);
     a.mode = 0;
+}
+
+// Integrating factors: precomputed in double (a table read by the column
+// pass) or evaluated per value in the state precision, as lin_func does.
+// AM_IF_AUTO takes the table except for FP32 with the reference's mask (the
+// parity mode, where the reference's own float exponentials are reproduced).
+inline bool use_if_table(const am_params &p)
+{
+    if (p.if_factors == AM_IF_DOUBLE) return true;
+    if (p.if_factors == AM_IF_FLOAT) return false;
+    return !(p.precision == AM_FP32 && p.dealias == AM_DEALIAS_REFERENCE);
+}
+
+// Table coefficients: wavenumber steps 2 pi / L and the operator in double
+// (the oracle's precision-form restatement uses the same expressions).
+inline LinCoef lin_coef(const am_params &p)
+{
+    LinCoef c;
+    c.kxs = 2.0 * M_PI / p.lx;
+    c.kys = 2.0 * M_PI / p.ly;
+    c.dt = p.dt;
+    c.alpha = p.alpha;
+    c.g0 = p.gamma0;
+    c.g2 = p.gamma2;
+    c.form = p.form;
+    return c;
 }
 
 // Pruned transforms.  Under the 1/2 rule every nonlinear term vanishes outside

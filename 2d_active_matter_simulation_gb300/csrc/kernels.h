@@ -18,6 +18,26 @@ struct LaunchShape {
                               // tiles (set-up column kernels) per CTA
 };
 
+// Coefficients of the integrating-factor table (k_lintab): wavenumber steps
+// 2 pi / L, parameters in double, operator form (am_form).
+struct LinCoef {
+    double kxs, kys, dt, alpha, g0, g2;
+    int form;
+};
+
+// Table entry {exp(L dt / 2), exp(L dt)} at half-plane index (kx, y): the
+// wavenumbers, L(k) and both exponentials in double, each rounded to T once.
+// L = -(1 - k^2)^2 - alpha (lin_func, ActFlow_V3-2.cu:1020-1033) or
+// -alpha - g0 k^2 - g2 k^4.
+template <typename T>
+AF_HD cpx<T> lintab_value(const LinCoef &c, int ny, int kx, int y)
+{
+    const double kxd = c.kxs * kx, kyd = c.kys * (y < ny / 2 + 1 ? y : y - ny);
+    const double k2 = kyd * kyd + kxd * kxd;
+    const double L = c.form == 0 ? -(1 - k2) * (1 - k2) - c.alpha : -c.alpha - c.g0 * k2 - c.g2 * k2 * k2;
+    return mk((T)exp(L * c.dt / 2), (T)exp(L * c.dt));
+}
+
 // CTAs of a step column-pass launch over ntp column tiles of W columns.
 inline int col_grid(const LaunchShape &s, int ntp, int W) { return (ntp * W + s.per_block - 1) / s.per_block; }
 
@@ -33,6 +53,7 @@ struct KernelTable {
     LaunchShape colfwd_shape[LOG_MAX + 1];
     void (*tile)(const cpx<T> *, cpx<T> *, int, int, int);    // [ny][nxh] -> tiled
     void (*untile)(const cpx<T> *, cpx<T> *, int, int, int);  // tiled -> [ny][nxh]
+    void (*lintab)(cpx<T> *, int, int, int, LinCoef);         // integrating-factor table
 };
 
 const KernelTable<float> &kernels_f32();

@@ -67,6 +67,23 @@ __global__ void k_untile(const cpx<T> *src, cpx<T> *dst, int ny, int nxh, int nt
     }
 }
 
+// Integrating factors {exp(L dt / 2), exp(L dt)} at every half-plane (kx, ky)
+// (lintab_value), tiled like the fields; padding columns zero.
+template <typename T>
+__global__ void k_lintab(cpx<T> *tab, int nx, int ny, int nt, LinCoef c)
+{
+    constexpr int W = Tile<T>::W;
+    const int nxh = nx / 2 + 1;
+    const size_t total = (size_t)nt * W * ny;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int cc = (int)(i % W);
+        const size_t rest = i / W;
+        const int y = (int)(rest % ny);
+        const int kx = (int)(rest / ny) * W + cc;
+        tab[i] = kx < nxh ? lintab_value<T>(c, ny, kx, y) : mk<T>(0, 0);
+    }
+}
+
 template <typename T, int LOG, int HI>
 struct Fill {
     template <int V>
@@ -107,6 +124,7 @@ void fill_common(KernelTable<T> &t)
 {
     t.tile = k_tile<T>;
     t.untile = k_untile<T>;
+    t.lintab = k_lintab<T>;
 }
 
 }  // namespace af

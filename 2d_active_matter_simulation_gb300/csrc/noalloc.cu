@@ -229,6 +229,7 @@ extern "C" am_status am_step_noalloc(const am_params *p, void *w_hat, double *me
     // the parameter checks of am_create: a non-positive box length makes the
     // wavenumber tables infinite and the state NaN
     if (!(p->lx > 0) || !(p->ly > 0) || !std::isfinite(p->dt)) return AM_ERR_ARG;
+    if (p->if_factors < AM_IF_AUTO || p->if_factors > AM_IF_DOUBLE) return AM_ERR_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     return p->precision == AM_FP64 ? run<double>(*p, w_hat, mean, nsteps, energy, st)
                                    : run<float>(*p, w_hat, mean, nsteps, energy, st);

@@ -79,7 +79,8 @@ struct SizeClass {
 // Bytes of one run's device block: 7 fields, side buffer, tables, energy
 // ring, scalars, each 256-byte aligned.
 struct RunLayout {
-    size_t fields, side, twx, twy, kx, ky, energy, sc, total;
+    size_t fields, lin, side, twx, twy, kx, ky, energy, sc, total;
+    bool has_lin;   // integrating-factor table (AM_IF_DOUBLE), one field
 };
 RunLayout run_layout(const am_params &p)
 {
@@ -89,6 +90,9 @@ RunLayout run_layout(const am_params &p)
     size_t o = 0;
     L.fields = o;
     o += align_up(7 * (size_t)nt * W * p.ny * sizeof(cpx<float>));
+    L.lin = o;
+    L.has_lin = use_if_table(p);
+    if (L.has_lin) o += align_up((size_t)nt * W * p.ny * sizeof(cpx<float>));
     L.side = o;
     o += align_up(side_bytes(p.ny));
     L.twx = o;
@@ -225,6 +229,7 @@ am_status am_ragged_create(const am_params *params, const long long *nsteps, int
         if (p.dealias < 0 || p.dealias > 2 || (p.form != AM_FORM_REFERENCE && p.form != AM_FORM_GENERAL))
             return AM_ERR_ARG;
         if (!(p.lx > 0) || !(p.ly > 0) || !(p.dt == p.dt) || nsteps[i] < 0) return AM_ERR_ARG;
+        if (p.if_factors < AM_IF_AUTO || p.if_factors > AM_IF_DOUBLE) return AM_ERR_ARG;
     }
     am_ragged *r = new (std::nothrow) am_ragged();
     if (!r) return AM_ERR_OOM;
@@ -305,6 +310,12 @@ am_status am_ragged_create(const am_params *params, const long long *nsteps, int
         set_side<float>(a, base + L.side, run.p.ny);
         a.sc = r->sc_all + i;
         a.energy = r->ering_all + (size_t)i * ECAP_R;
+        if (L.has_lin) {
+            cpx<float> *lin = reinterpret_cast<cpx<float> *>(base + L.lin);
+            kernels_f32().lintab<<<1024, 256, 0, r->stream>>>(lin, run.p.nx, run.p.ny, t.nt, lin_coef(run.p));
+            if (cudaGetLastError() != cudaSuccess) return fail(AM_ERR_CUDA);
+            a.lintab = lin;
+        }
         if (cudaMemcpyAsync(base + L.twx, t.twx.data(), t.twx.size() * sizeof(cpx<float>), cudaMemcpyHostToDevice,
                             r->stream) ||
             cudaMemcpyAsync(base + L.twy, t.twy.data(), t.twy.size() * sizeof(cpx<float>), cudaMemcpyHostToDevice,

@@ -57,6 +57,9 @@ struct StepArgs {
     const cpx<T> *twy;              // exp(-2 pi i m / Ny), m < Ny
     const T *kxt;                   // kx wavenumbers, nt * W entries (0 past Nx/2)
     const T *kyt;                   // ky wavenumbers in FFT order, Ny entries
+    const cpx<T> *lintab;           // integrating factors {exp(L dt / 2), exp(L dt)} per (kx, ky),
+                                    // tiled like the fields, computed in double and rounded
+                                    // (nullptr: evaluated per value in T, as lin_func)
     T *rowp;                        // per-row sums [3][Ny]: |u|^2, |u|^2 ux, |u|^2 uy
     Scalars *sc;
     double *energy;                 // energy per step, ring of ecap entries
@@ -749,21 +752,33 @@ struct ColPass {
                 const int iy = j + r * TPC;
                 const size_t g = cbase + (size_t)iy * W;
                 const cpx<T> n = nl[r], o = av[r];
-                // exp(L dt / 2) at (kx, ky); exp(L dt) is formed as its square.
-                // ky(-iy) = -ky(iy) exactly, so the mirror shares this value.
-                const T e2 = MODE == 4 ? (T)0 : lin_at(a, kxv, iy, dt / 2);
-                cpx<T> w = MODE == 1 ? scale(o, e2 * e2) : accv[r];   // stage 1: w_new = w_old * lin
+                // e2 = exp(L dt / 2) and e1 = exp(L dt) at (kx, ky): from the
+                // table (double, rounded once), or e2 evaluated here in T and
+                // e1 formed as its square.  ky(-iy) = -ky(iy) exactly, so the
+                // mirror shares these values.
+                T e2 = 0, e1 = 0;
+                if constexpr (MODE != 4) {
+                    if (a.lintab) {
+                        const cpx<T> f = active ? a.lintab[g] : mk<T>(0, 0);
+                        e2 = f.x;
+                        e1 = f.y;
+                    } else {
+                        e2 = lin_at(a, kxv, iy, dt / 2);
+                        e1 = e2 * e2;
+                    }
+                }
+                cpx<T> w = MODE == 1 ? scale(o, e1) : accv[r];   // stage 1: w_new = w_old * lin
                 if (c0 && iy != 0 && iy != ny / 2) {
                     // Hermitian repair with the mirror value w_new(-ky)
                     const int my = ny - iy;
                     cpx<T> b;
-                    if constexpr (MODE == 1) b = scale(PM ? mir[my] : a.u0[cbase + (size_t)my * W], e2 * e2);
+                    if constexpr (MODE == 1) b = scale(PM ? mir[my] : a.u0[cbase + (size_t)my * W], e1);
                     else b = PM ? mir[my] : hin[my];
                     if (iy < ny / 2) w = mk((T)0.5f * (w.x + b.x), (T)0.5f * (w.y - b.y));
                     else w = conj(mk((T)0.5f * (b.x + w.x), (T)0.5f * (b.y - w.y)));
                 }
                 if constexpr (MODE == 1) {
-                    T f = dt / 6 * (e2 * e2);
+                    T f = dt / 6 * e1;
                     w = mk(w.x + f * n.x, w.y + f * n.y);
                     av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), e2);
                 } else if constexpr (MODE == 2) {
@@ -773,7 +788,7 @@ struct ColPass {
                 } else if constexpr (MODE == 3) {
                     T f = dt / 3 * e2;
                     w = mk(w.x + f * n.x, w.y + f * n.y);
-                    av[r] = scale(mk(o.x + dt * n.x, o.y + dt * n.y), e2 * e2);
+                    av[r] = scale(mk(o.x + dt * n.x, o.y + dt * n.y), e1);
                 } else {
                     w = mk(w.x + dt / 6 * n.x, w.y + dt / 6 * n.y);
                     av[r] = w;   // next step: w_old = w_appr = w_new

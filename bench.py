@@ -126,9 +126,39 @@ def apply_preset(cfg, precision):
                 f"{'1/2-rule' if p['dealias'] == 'half' else 'reference-mask'} dealiasing, band-limited seed {SEED}")
 
 
-# DRAM read + write bytes per launch of each pass for this workload, from the
-# ncu capture summarised in profiles/k_row_k_col_2048_fp32_full.md
-NCU_TRAFFIC = {"row": 25.417e6 + 0.058e6, "col": 25.496e6 + 0.193e6}
+def workload_config():
+    """The workload both arms time (the reference arm prints the same dict)."""
+    n, _ = world()
+    return {"workload": WORKLOAD, "nx": NX, "ny": NY, "dt": PARAMS["dt"], "dealias": PARAMS["dealias"],
+            "precision": PRECISION, "seed": SEED,
+            "parallelism": "single GPU" if n == 1 else f"{n} independent replicas (one simulation per GPU, no exchange)",
+            "l2": "flushed before every timed step (256 MB write)"}
+
+
+def ncu_traffic(kernel_key):
+    """DRAM read + write bytes per launch of the dominant kernel for this
+    workload, from the committed ncu summary of the current build
+    (profiles/ncu_traffic_<workload>.txt, lines "<kernel>_dram_bytes_per_launch:
+    <bytes>" and "build: <commit>").  None where no capture covers the workload."""
+    name = f"ncu_traffic_{NX}x{NY}_{PRECISION}.txt"
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None, None
+    vals, build = {}, None
+    with open(path) as f:
+        for line in f:
+            if ":" not in line:
+                continue
+            k, v = line.split(":", 1)
+            k, v = k.strip(), v.strip()
+            if k == "build":
+                build = v
+            elif k.endswith("_dram_bytes_per_launch"):
+                try:
+                    vals[k[: -len("_dram_bytes_per_launch")]] = float(v.split()[0])
+                except ValueError:
+                    pass
+    return vals.get(kernel_key), f"profiles/{name} (build {build})" if build else f"profiles/{name}"
 
 
 def peaks():
@@ -197,9 +227,8 @@ def oracle_steps(nsteps, threads=0):
     """Time `nsteps` full oracle steps of the workload on host cores."""
     import numpy as np
     import oracle
-    import importlib
-    am = importlib.import_module("2d_active_matter_simulation_gb300")
-    w0 = am.ic_bandlimited(NX, NY, SEED).astype(np.complex64 if PRECISION == "fp32" else np.complex128)
+    from oracle.ic import bandlimited
+    w0 = bandlimited(NX, NY, SEED).astype(np.complex64 if PRECISION == "fp32" else np.complex128)
     p = oracle.make_params(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"],
                            PARAMS["beta"], PARAMS["gamma0"], PARAMS["gamma2"], dealias=PARAMS["dealias"])
     t = time.perf_counter()
@@ -225,11 +254,12 @@ def run_reference(args):
     out = {
         "impl": "reference", "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if PRECISION == "fp32" else "f64", "data": "synthetic",
+        "config": workload_config(),
         "cpu_baseline": {"value": value, "unit": "grid-point-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full 2048^2 steps of the oracle (C restatement of "
-                                   "ActFlow_V3-2.cu's step, OpenMP), FP32"},
+                         "sample": f"{args.steps} full {NX}x{NY} steps of the oracle (C restatement of "
+                                   f"ActFlow_V3-2.cu's step, OpenMP), {PRECISION.upper()}"},
         "e2e": {"value": value, "unit": "grid-point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -351,19 +381,34 @@ def run_ours(args):
                "sample": f"{n_cpu} full 2048^2 steps of the oracle (C restatement of the reference step, "
                          f"OpenMP, FP32), {t_cpu:.1f} s"}
 
+    # ---- the reference's own cuFFT build and the cuFFT floor on this GPU
+    # (the headline workload only; rank 0 of a single-GPU run)
+    compare = {}
+    if not args.no_compare and nrep == 1 and NX == 2048 and NY == 2048 and PRECISION == "fp32":
+        from baseline import reference_gpu
+        for key_, fn in (("reference_gpu", reference_gpu.time_reference), ("cufft_floor", reference_gpu.time_floor)):
+            try:
+                compare[key_] = fn(NX, steps=200)
+            except Exception as exc:   # a comparator that fails is reported, never fatal
+                compare[key_] = {"unavailable": f"{type(exc).__name__}: {exc}"[:300]}
+        for key_ in ("reference_gpu", "cufft_floor"):
+            if "value" in compare.get(key_, {}):
+                compare[key_]["speedup_of_e2e"] = e2e_value / compare[key_]["value"]
+                compare[key_]["speedup_of_value"] = value / compare[key_]["value"]
+
+    traffic, traffic_src = ncu_traffic(key) if kxc == NX // 4 else (None, None)
     out = {
         "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s", "n_gpus": nrep,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if PRECISION == "fp32" else "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "dt": PARAMS["dt"], "dealias": PARAMS["dealias"],
-                   "parallelism": "single GPU" if world()[0] == 1 else
-                   f"{world()[0]} independent replicas (one simulation per GPU, no exchange)",
-                   "l2": "flushed before every timed step (256 MB write)",
-                   "timing": "CUDA events on the solver stream, one CUDA graph (8 kernels) per step",
-                   "column_shape": tune[2], "autotune_ms_per_step": {"wide": tune[0], "narrow": tune[1]}},
+        "config": workload_config(),
+        "timing": "CUDA events on the solver stream, one CUDA graph (8 kernels) per step",
+        "tuning": {"column_shape": tune[2], "autotune_ms_per_step": {"wide": tune[0], "narrow": tune[1]}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": NCU_TRAFFIC[key] if (NX == 2048 and PRECISION == "fp32" and kxc == NX // 4) else None, "kernel": dom, "algorithmic_bytes_per_launch": dom_bytes,
+                     "traffic": traffic, "traffic_source": traffic_src, "kernel": dom,
+                     "algorithmic_bytes_per_launch": dom_bytes,
                      "avg_launch_ms": dom_ms, "peak_source": peak_kind,
+                     "kernel_timing": "CUDA events recorded inside the step's graph around each kernel",
                      "row_pass_ms": row_avg, "column_pass_ms": col_avg,
                      "step_achieved_gbs": step_achieved, "step_frac": step_achieved / peak,
                      "kx_carried": kxc, "pruned": kxc < NX // 2,
@@ -376,19 +421,27 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk,
     }
+    out.update(compare)
     if world()[1] == 0:
         print(json.dumps(out), flush=True)
 
 
 def run_accuracy(args):
-    """Precision form: FP32 against the FP64 path from the same seeded field.
+    """Precision form: the FP32 path (bulk FFT and products in FP32, integrating
+    factors computed in double and rounded, mean flow and reductions in double
+    or compensated FP32) against the FP64 path.
 
-    Short horizon: relative L2 of w_hat after 200 steps.  Long horizon: the
-    time-mean energy over the second half of the run and the time-averaged
-    shell spectrum (snapshots every 200 steps in the second half; the flow is
-    chaotic, so the spectra agree only statistically).  The FP64
-    path is the solver's own double-precision build, which agrees with the
-    CPU FP64 oracle to 1e-10 over the parity tests' horizons."""
+    Short horizon: relative L2 of w_hat after 200 steps from the seeded field.
+    Long horizon: the time-mean energy and the time-averaged shell spectrum
+    (snapshots every 200 steps) over a window of the saturated flow.  With
+    --acc-spinup S the FP64 path first runs S steps from the seeded field and
+    every long run starts from that state (FP32 from it rounded); the window is
+    then the whole run of --acc-steps steps.  Without it the window is the
+    second half of a run from the seeded field.  The flow is chaotic, so the
+    two precisions agree only statistically: --acc-twins FP64 runs from the
+    same state perturbed by one part in 1e12 (a different seeded perturbation
+    per twin) measure the spread of the flow itself, and the FP32 differences
+    are read against the largest twin difference (the envelope)."""
     import importlib
 
     import numpy as np
@@ -397,57 +450,92 @@ def run_accuracy(args):
     spec = importlib.import_module("2d_active_matter_simulation_gb300.spectrum")
     n_total = args.acc_steps
     w0 = am.ic_bandlimited(NX, NY, SEED)
-    res = {}
+
+    def solver(prec):
+        return am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"],
+                         PARAMS["beta"], gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"],
+                         dealias=PARAMS["dealias"], precision=prec)
+
+    res = {"if_factors": "double, rounded (auto)"}
+    # short horizon from the seeded field
+    short = {}
+    for prec in ("fp32", "fp64"):
+        sim = solver(prec)
+        sim.set_state(w0 if prec == "fp64" else w0.astype(np.complex64))
+        sim.step(200)
+        short[prec] = sim.get_state()[0].astype(np.complex128)
+        sim.close()
+    res["short_horizon_steps"] = 200
+    res["w_rel_l2_200"] = float(np.linalg.norm(short["fp32"] - short["fp64"]) / np.linalg.norm(short["fp64"]))
+
+    # start of the long runs
+    t0 = time.perf_counter()
+    if args.acc_spinup > 0:
+        sim = solver("fp64")
+        sim.set_state(w0)
+        sim.step(args.acc_spinup, energy=False)
+        s0, m0 = sim.get_state()
+        sim.close()
+        window_from = 0
+    else:
+        s0, m0 = w0, np.zeros(2)
+        window_from = n_total // 2
+    res["spinup_steps"] = args.acc_spinup
+    res["spinup_seconds"] = time.perf_counter() - t0
+
+    rng = np.random.default_rng(1234)
     runs = {}
-    # "twin": FP64 from the same field perturbed by one part in 1e12 -- the
-    # spread of the chaotic flow itself, against which the FP32 vs FP64
-    # long-horizon differences are read
-    w0_twin = w0 * (1.0 + 1e-12)
-    for prec in ("fp32", "fp64", "twin"):
-        sim = am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"],
-                        PARAMS["beta"], gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"],
-                        dealias=PARAMS["dealias"], precision="fp32" if prec == "fp32" else "fp64")
-        sim.set_state(w0 if prec == "fp64" else w0_twin if prec == "twin" else w0.astype(np.complex64))
-        t0 = time.perf_counter()
-        e = [sim.step(200)]
-        w200, _ = sim.get_state()
-        specs = []
-        done = 200
+    names = ["fp32", "fp64"] + [f"twin{i}" for i in range(args.acc_twins)]
+    for name in names:
+        if name.startswith("twin"):
+            # one part in 1e12 per mode, Hermitian on the kx = 0 column
+            r = rng.standard_normal(s0.shape)
+            r[:, 0] = 0.5 * (r[:, 0] + r[(-np.arange(NY)) % NY, 0])
+            start_w = s0 * (1.0 + 1e-12 * r)
+        else:
+            start_w = s0 if name == "fp64" else s0.astype(np.complex64)
+        sim = solver("fp32" if name == "fp32" else "fp64")
+        sim.set_state(start_w, m0)
+        t1 = time.perf_counter()
+        e, specs, done = [], [], 0
         while done < n_total:
             k = min(200, n_total - done)
             e.append(sim.step(k))
             done += k
-            if done >= n_total // 2:
+            if done > window_from:
                 w, m = sim.get_state()
                 specs.append(spec.energy_spectrum(w.astype(np.complex128), m, NX, NY, PARAMS["lx"], PARAMS["ly"])[1])
-        dt_run = time.perf_counter() - t0
+        runs[name] = dict(energy=np.concatenate(e), spec=np.mean(specs, axis=0), seconds=time.perf_counter() - t1)
         sim.close()
-        runs[prec] = dict(w200=w200.astype(np.complex128), energy=np.concatenate(e),
-                          spec=np.mean(specs, axis=0) if specs else None, seconds=dt_run)
-    a, b = runs["fp32"], runs["fp64"]
-    half = len(b["energy"]) // 2
-    res["short_horizon_steps"] = 200
-    res["w_rel_l2_200"] = float(np.linalg.norm(a["w200"] - b["w200"]) / np.linalg.norm(b["w200"]))
+
+    kmax = NX // 4   # shells carried by the 1/2 rule
+    ref = runs["fp64"]
+    e_ref = float(np.mean(ref["energy"][window_from:]))
+    s_ref = ref["spec"][: kmax + 1]
+
+    def diffs(run):
+        me = float(np.mean(run["energy"][window_from:]))
+        sa = run["spec"][: kmax + 1]
+        return {"mean_energy": me, "mean_energy_rel_diff": abs(me / e_ref - 1),
+                "spectrum_l1_rel_diff": float(np.sum(np.abs(sa - s_ref)) / np.sum(s_ref)),
+                "spectrum_max_rel_diff": spec.spectrum_rel_error(run["spec"], ref["spec"], kmax)}
+
     res["long_horizon_steps"] = n_total
-    res["mean_energy_fp32"] = float(np.mean(a["energy"][half:]))
-    res["mean_energy_fp64"] = float(np.mean(b["energy"][half:]))
-    res["mean_energy_rel_diff"] = abs(res["mean_energy_fp32"] / res["mean_energy_fp64"] - 1)
-    if a["spec"] is not None:
-        kmax = NX // 4   # shells carried by the 1/2 rule
-        res["spectrum_max_rel_diff"] = spec.spectrum_rel_error(a["spec"], b["spec"], kmax)
-        sa, sb = a["spec"][: kmax + 1], b["spec"][: kmax + 1]
-        res["spectrum_l1_rel_diff"] = float(np.sum(np.abs(sa - sb)) / np.sum(sb))
-        res["spectrum_snapshots"] = (n_total - n_total // 2) // 200
-    t = runs["twin"]
-    res["twin_w_rel_l2_200"] = float(np.linalg.norm(t["w200"] - b["w200"]) / np.linalg.norm(b["w200"]))
-    res["twin_mean_energy_rel_diff"] = abs(float(np.mean(t["energy"][half:])) / res["mean_energy_fp64"] - 1)
-    if t["spec"] is not None and b["spec"] is not None:
-        st, s64 = t["spec"][: NX // 4 + 1], b["spec"][: NX // 4 + 1]
-        res["twin_spectrum_l1_rel_diff"] = float(np.sum(np.abs(st - s64)) / np.sum(s64))
-    res["energy_fp64_first_last"] = [float(b["energy"][0]), float(b["energy"][half]), float(b["energy"][-1])]
-    res["seconds_fp32"] = a["seconds"]
-    res["seconds_fp64"] = b["seconds"]
-    res["gps_fp64"] = NX * NY * n_total / b["seconds"]
+    res["window_steps"] = [args.acc_spinup + window_from, args.acc_spinup + n_total]
+    res["mean_energy_fp64"] = e_ref
+    res["fp32"] = diffs(runs["fp32"])
+    res["twins"] = [diffs(runs[f"twin{i}"]) for i in range(args.acc_twins)]
+    if res["twins"]:
+        env_e = max(t["mean_energy_rel_diff"] for t in res["twins"])
+        env_s = max(t["spectrum_l1_rel_diff"] for t in res["twins"])
+        res["twin_envelope"] = {"mean_energy_rel_diff": env_e, "spectrum_l1_rel_diff": env_s}
+        res["fp32_within_target"] = {
+            "mean_energy": res["fp32"]["mean_energy_rel_diff"] <= max(0.01, env_e),
+            "spectrum_l1": res["fp32"]["spectrum_l1_rel_diff"] <= max(0.01, env_s)}
+    res["energy_fp64_first_last"] = [float(ref["energy"][0]), float(ref["energy"][-1])]
+    res["seconds"] = {k: v["seconds"] for k, v in runs.items()}
+    res["gps_fp64"] = NX * NY * n_total / runs["fp64"]["seconds"]
+    res["gps_fp32"] = NX * NY * n_total / runs["fp32"]["seconds"]
     print(json.dumps({"accuracy": res, "config": {"workload": WORKLOAD}}), flush=True)
 
 
@@ -655,8 +743,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip timing the reference's cuFFT build and the cuFFT floor")
     ap.add_argument("--accuracy", action="store_true", help="FP32 vs FP64 precision-form check instead")
-    ap.add_argument("--acc-steps", type=int, default=20000)
+    ap.add_argument("--acc-steps", type=int, default=20000, help="accuracy: steps of each long run")
+    ap.add_argument("--acc-spinup", type=int, default=0, help="accuracy: FP64 steps before the long runs")
+    ap.add_argument("--acc-twins", type=int, default=4, help="accuracy: perturbed FP64 runs (chaotic spread)")
     ap.add_argument("--config", type=int, default=1, choices=sorted(PRESETS))
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="config 4: arrival window")

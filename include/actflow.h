@@ -57,6 +57,15 @@ typedef enum { AM_DEALIAS_REFERENCE = 0, AM_DEALIAS_HALF = 1, AM_DEALIAS_NONE = 
  * mean-flow factor exp(-alpha dt) -- the dimensional form of the same model. */
 typedef enum { AM_FORM_REFERENCE = 0, AM_FORM_GENERAL = 1 } am_form;
 
+/* Integrating factors exp(L(k) dt) and exp(L(k) dt / 2).  FLOAT evaluates them
+ * per value in the state's precision inside the step, as lin_func does
+ * (ActFlow_V3-2.cu:1020-1033, float exp); DOUBLE precomputes them once per
+ * simulation in double (double wavenumbers and parameters) and rounds them to
+ * the state's precision -- the precision form, where FP32 runs keep the
+ * exponentials at FP64 accuracy.  AUTO: DOUBLE, except FP32 with the
+ * reference's mask (the parity mode), which uses FLOAT like the reference. */
+typedef enum { AM_IF_AUTO = 0, AM_IF_FLOAT = 1, AM_IF_DOUBLE = 2 } am_if_factors;
+
 typedef struct am_params {
     int nx, ny;              /* grid; powers of two, 8..4096 (FP64: Ny <= 4096) */
     double lx, ly;           /* box lengths */
@@ -66,7 +75,8 @@ typedef struct am_params {
     int form;                /* am_form */
     int dealias;             /* am_dealias */
     int precision;           /* am_precision */
-    int reserved[5];         /* must be zero */
+    int if_factors;          /* am_if_factors; 0 = AM_IF_AUTO */
+    int reserved[4];         /* must be zero */
 } am_params;
 
 typedef struct am_handle am_handle;
@@ -113,10 +123,13 @@ am_status am_step(am_handle *h, int nsteps, double *energy, int *nan_step);
 am_status am_step_async(am_handle *h, int nsteps);
 am_status am_sync(am_handle *h);
 
-/* Advance nsteps steps launching the 8 kernels of each step individually with
- * CUDA events between them on the handle's stream, and add each kernel's
- * duration (milliseconds) to row_ms[stage-1] / col_ms[stage-1] (stage 1..4).
- * For measurement; am_step is the production path (one CUDA graph per step). */
+/* Advance nsteps steps as am_step does (one CUDA graph per step, the 8
+ * kernels back to back), with a timing event recorded inside the graph before
+ * and after each kernel, and add each kernel's duration (milliseconds) to
+ * row_ms[stage-1] / col_ms[stage-1] (stage 1..4).  The host waits for every
+ * step, so use it for measurement; am_step is the production path.  No
+ * counterpart in the reference, which times only its whole loop
+ * (ActFlow_V3-2.cu:713, 841-843). */
 am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double col_ms[4]);
 
 /* Advance nsteps steps without allocating anything.  No counterpart in the
@@ -140,7 +153,9 @@ am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double co
  * has been through cudaDeviceReset must not be used with this entry point again
  * (the reset destroyed the array).  The work is enqueued on `stream` (a
  * cudaStream_t, NULL = default stream) and the call returns without waiting; it
- * runs the full transforms and reports no NaN (check mean or the energies).
+ * runs the full transforms, evaluates the integrating factors per value in the
+ * state's precision whatever p->if_factors asks (a table would not fit the
+ * array), and reports no NaN (check mean or the energies).
  * Calls share the array: calls that overlap on the GPU race and must be
  * serialised. */
 am_status am_step_noalloc(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy, void *stream);

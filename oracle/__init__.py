@@ -24,7 +24,7 @@ class OrcParams(ctypes.Structure):
         ("lx", ctypes.c_double), ("ly", ctypes.c_double), ("dt", ctypes.c_double),
         ("lam", ctypes.c_double), ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
         ("gamma0", ctypes.c_double), ("gamma2", ctypes.c_double),
-        ("form", ctypes.c_int), ("dealias", ctypes.c_int),
+        ("form", ctypes.c_int), ("dealias", ctypes.c_int), ("if_double", ctypes.c_int),
     ]
 
 
@@ -58,11 +58,15 @@ def lib():
     return _lib
 
 
-def make_params(nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None, dealias="reference"):
+def make_params(nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None, dealias="reference",
+                if_double=False):
+    """if_double: integrating factors evaluated in double and rounded once to
+    the run's precision (the solver's precision form) instead of in that
+    precision as lin_func does."""
     form = 0 if gamma0 is None else 1
     return OrcParams(nx, ny, lx, ly, dt, lam, alpha, beta,
                      0.0 if gamma0 is None else gamma0, 0.0 if gamma2 is None else gamma2,
-                     form, DEALIAS[dealias] if isinstance(dealias, str) else int(dealias))
+                     form, DEALIAS[dealias] if isinstance(dealias, str) else int(dealias), 1 if if_double else 0)
 
 
 def run(params, w_hat, mean, nsteps, precision="f64", nthreads=0):

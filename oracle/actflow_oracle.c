@@ -33,6 +33,8 @@ typedef struct {
     double gamma0, gamma2;
     int form;    /* 0: reference operator -(1-k^2)^2 - alpha; 1: -alpha - g0 k^2 - g2 k^4 */
     int dealias; /* 0: reference mask (int32 arithmetic), 1: isotropic 1/2 rule, 2: none */
+    int if_double; /* 0: integrating factors evaluated in REAL (lin_func); 1: in double from
+                    * double wavenumbers and parameters, then rounded to REAL */
 } orc_params;
 
 /* Dealiasing mask value at half-plane index (ix, iy).

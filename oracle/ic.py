@@ -3,7 +3,8 @@
 TEST INFRASTRUCTURE ONLY: this module is the checker's copy of the initial-field
 generators.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg
 of ``bench.py`` may import it; the product generates its initial fields in C++
-(``csrc/host/ic.cpp``) and this file exists to check that code.
+(``am_ic_bandlimited`` in ``csrc/actflow_api.cu``) and this file exists to
+check that code.
 
 Two generators are restated here.
 

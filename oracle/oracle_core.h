@@ -248,6 +248,19 @@ static int F(solver_init)(F(solver) * s, const orc_params *prm)
      * mean-flow scalars, ActFlow_V3-2.cu:704-705).  The general form replaces
      * -(1-k^2)^2 - alpha by -alpha - Gamma0 k^2 - Gamma2 k^4. */
     for (int c = 0; c < s->size; c++) {
+        if (prm->if_double) {
+            /* the precision form: exp(L dt) and exp(L dt / 2) in double from
+             * the double wavenumbers and parameters, rounded to REAL once */
+            int row = c / nxh, col = c % nxh;
+            int n = row < ny / 2 + 1 ? row : row - ny;
+            double kyd = 2.0 * M_PI / prm->ly * n, kxd = 2.0 * M_PI / prm->lx * col;
+            double k2d = kyd * kyd + kxd * kxd;
+            double Ld = prm->form == 0 ? -(1 - k2d) * (1 - k2d) - prm->alpha
+                                       : -prm->alpha - prm->gamma0 * k2d - prm->gamma2 * k2d * k2d;
+            s->lin[c] = (REAL)exp(Ld * prm->dt);
+            s->lin2[c] = (REAL)exp(Ld * prm->dt / 2);
+            continue;
+        }
         REAL k2 = s->k2[c];
         REAL L;
         if (prm->form == 0)

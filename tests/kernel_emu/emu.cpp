@@ -54,6 +54,16 @@ struct Runner {
         a.u0 = u0.data(); a.acc = acc.data(); a.fa = fa.data(); a.fx = fx.data(); a.fy = fy.data();
         a.P = P.data(); a.Q = Q.data(); a.twx = t.twx.data(); a.twy = t.twy.data();
         a.kxt = t.kx.data(); a.kyt = t.ky.data(); set_side<T>(a, rowp.data(), ny); a.sc = &sc; a.energy = en.data();
+        // integrating-factor table, as the C ABI builds it (k_lintab) when the
+        // parameters ask for factors computed in double
+        std::vector<cpx<T>> lin;
+        if (use_if_table(p)) {
+            lin.assign(fsz, mk<T>(0, 0));
+            const LinCoef c = lin_coef(p);
+            for (int y = 0; y < ny; y++)
+                for (int k = 0; k < t.nxh; k++) lin[tidx<T>(k, y, ny)] = lintab_value<T>(c, ny, k, y);
+            a.lintab = lin.data();
+        }
         // tile the input
         for (int y = 0; y < ny; y++)
             for (int k = 0; k < t.nxh; k++) {

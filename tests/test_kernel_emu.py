@@ -132,3 +132,24 @@ def test_emulated_production_lengths(am, orc, emu, n, prec, kind):
     assert np.linalg.norm(w - wo) / np.linalg.norm(wo) < tol
     assert np.abs(m - mo).max() <= tol * np.abs(mo).max()
     assert np.abs(e - eo).max() <= tol * np.abs(eo).max()
+
+
+@pytest.mark.parametrize("if_factors", ["float", "double"])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_emulated_integrating_factor_modes(am, orc, emu, if_factors, prec):
+    """Both ways of forming exp(L dt) and exp(L dt / 2): per value in the
+    state's precision (lin_func) and the table computed in double and rounded
+    once (the precision form), each against the oracle that forms them the
+    same way."""
+    nx, ny = 64, 128
+    w0 = am.ic_bandlimited(nx, ny, seed=23, kmax=10.0, rms=2.0)
+    p = am.Params(nx, ny, 6.283185307179586, 6.283185307179586, 2e-3, 3.5, -0.8, 0.01, -0.045, 2.5e-5, 1,
+                  am.DEALIAS["half"], prec, am.IF_FACTORS[if_factors])
+    w, m, e = _emu_run(am, emu, p, w0, (20.0, -5.0), 3)
+    op = orc.make_params(nx, ny, 6.283185307179586, 6.283185307179586, 2e-3, 3.5, -0.8, 0.01, -0.045, 2.5e-5,
+                         dealias="half", if_double=if_factors == "double")
+    wo, mo, eo = orc.run(op, w0 if prec else w0.astype(np.complex64), (20.0, -5.0), 3, "f64" if prec else "f32")
+    tol = 1e-13 if prec else 2e-6
+    assert np.linalg.norm(w - wo) / np.linalg.norm(wo) < tol
+    assert np.abs(m - mo).max() <= tol * np.abs(mo).max()
+    assert np.abs(e - eo).max() <= tol * np.abs(eo).max()

@@ -104,6 +104,7 @@ def _load():
         "am_step_async": ([hp, ctypes.c_int], ctypes.c_int),
         "am_sync": ([hp], ctypes.c_int),
         "am_step_profiled": ([hp, ctypes.c_int, dp, dp], ctypes.c_int),
+        "am_row_passes_async": ([hp, ctypes.c_int], ctypes.c_int),
         "am_step_noalloc": ([ctypes.POINTER(Params), vp, vp, ctypes.c_int, vp, vp], ctypes.c_int),
         "am_launches_per_step": ([hp], ctypes.c_int),
         "am_device_bytes": ([hp], ctypes.c_longlong),
@@ -157,7 +158,7 @@ lib = _load()
 # Every symbol include/actflow.h declares (checked by the CPU test suite).
 EXPORTED = [
     "am_create", "am_destroy", "am_set_stream", "am_set_state", "am_set_state_real", "am_get_state",
-    "am_step", "am_step_async", "am_sync", "am_step_profiled", "am_step_noalloc", "am_launches_per_step", "am_device_bytes", "am_kx_carried",
+    "am_step", "am_step_async", "am_sync", "am_step_profiled", "am_row_passes_async", "am_step_noalloc", "am_launches_per_step", "am_device_bytes", "am_kx_carried",
     "am_status_string",
     "am_last_error", "am_mask_value", "am_ic_bandlimited", "am_spec_read", "am_write_snapshot",
     "am_read_snapshot", "am_append_energy", "am_cli_main", "am_batch_create", "am_batch_destroy",
@@ -255,6 +256,10 @@ class Solver:
         c = np.zeros(4)
         _check(lib.am_step_profiled(self.h, nsteps, _dptr(r), _dptr(c)), self.h, "am_step_profiled")
         return r, c
+
+    def row_passes_async(self, reps=1):
+        """Enqueue reps x the step's four row passes alone (for timing; state unchanged)."""
+        _check(lib.am_row_passes_async(self.h, reps), self.h, "am_row_passes_async")
 
     @property
     def launches_per_step(self):

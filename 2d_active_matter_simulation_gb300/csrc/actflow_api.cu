@@ -57,8 +57,8 @@ struct am_handle {
     double *rowp = nullptr, *energy = nullptr;
     Scalars *sc = nullptr;
     long long bytes = 0;
-    // graph of one step
-    cudaGraphExec_t graph = nullptr;
+    // graph of one step; graph of the step's four row passes alone (measurement)
+    cudaGraphExec_t graph = nullptr, graph_rows = nullptr;
     bool state_loaded = false;
     std::string err;
     // kernel arguments (scalar part filled at create)
@@ -228,6 +228,24 @@ static am_status build_graph(am_handle *h)
     return AM_OK;
 }
 
+// The four row passes of a step alone, as a graph (am_row_passes_async).
+template <typename T>
+static am_status build_rows_graph(am_handle *h)
+{
+    if (h->graph_rows) return AM_OK;
+    cudaGraph_t g;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    am_status st = AM_OK;
+    for (int s = 1; s <= 4 && !st; s++) st = launch_row<T>(h);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (st) return st;
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&h->graph_rows, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    return AM_OK;
+}
+
 static am_status reset_scalars(am_handle *h, const double mean[2])
 {
     Scalars s{};
@@ -254,6 +272,10 @@ static void choose_pruning(am_handle *h, bool on)
     if (a.ntp != old && h->graph) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
+    }
+    if (a.ntp != old && h->graph_rows) {
+        cudaGraphExecDestroy(h->graph_rows);
+        h->graph_rows = nullptr;
     }
 }
 
@@ -474,6 +496,7 @@ am_status am_destroy(am_handle *h)
 {
     if (!h) return AM_OK;
     if (h->graph) cudaGraphExecDestroy(h->graph);
+    if (h->graph_rows) cudaGraphExecDestroy(h->graph_rows);
     // Stream-ordered frees: the memory returns to the pool once the handle's
     // own work is done, without waiting for other streams of the device.
     void *ptrs[] = {h->u0, h->acc, h->fa, h->fx, h->fy, h->P, h->Q, h->stage, h->twx, h->twy,
@@ -493,6 +516,10 @@ am_status am_set_stream(am_handle *h, void *stream)
     if (h->graph) {
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;
+    }
+    if (h->graph_rows) {
+        cudaGraphExecDestroy(h->graph_rows);
+        h->graph_rows = nullptr;
     }
     if (stream) {
         if (h->own_stream) cudaStreamDestroy(h->stream);
@@ -608,6 +635,16 @@ am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double co
     for (auto &e : ev)
         if (e) cudaEventDestroy(e);
     return st;
+}
+
+am_status am_row_passes_async(am_handle *h, int reps)
+{
+    if (!h || reps < 0) return AM_ERR_ARG;
+    if (!h->state_loaded) return AM_ERR_ARG;
+    am_status st = h->fp64 ? build_rows_graph<double>(h) : build_rows_graph<float>(h);
+    if (st) return st;
+    for (int i = 0; i < reps; i++) CK(h, cudaGraphLaunch(h->graph_rows, h->stream));
+    return AM_OK;
 }
 
 am_status am_set_column_shape(int precision, int ny, int shape)

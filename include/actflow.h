@@ -132,6 +132,13 @@ am_status am_sync(am_handle *h);
  * (ActFlow_V3-2.cu:713, 841-843). */
 am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double col_ms[4]);
 
+/* Enqueue reps times the four row passes of one step, as one CUDA graph, on
+ * the handle's stream and return without waiting.  For measurement: a row
+ * pass reads the stage input and writes only the products and row sums, which
+ * the next step's row pass rewrites before any column pass reads them, so the
+ * state is left as it was.  No counterpart in the reference. */
+am_status am_row_passes_async(am_handle *h, int reps);
+
 /* Advance nsteps steps without allocating anything.  No counterpart in the
  * reference: it exists for callers that may not allocate device memory -- a
  * plug-in whose host application owns the device-memory budget, or a real-time

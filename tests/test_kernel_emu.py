@@ -105,7 +105,8 @@ def test_emulated_pruned_half_rule(am, orc, emu, n, prec):
 
 
 @pytest.mark.parametrize("n,kind", [((2048, 16), "full"), ((2048, 16), "pruned"), ((16, 2048), "full"),
-                                    ((16, 2048), "pruned"), ((4096, 8), "full"), ((8, 4096), "full")])
+                                    ((16, 2048), "pruned"), ((4096, 8), "full"), ((8, 4096), "full"),
+                                    ((512, 8), "pruned"), ((1024, 8), "full")])
 @pytest.mark.parametrize("prec", [0, 1])
 def test_emulated_production_lengths(am, orc, emu, n, prec, kind):
     """The row kernel at Nx = 2048 and the column kernel at Ny = 2048 (the

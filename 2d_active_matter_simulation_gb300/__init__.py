@@ -55,7 +55,8 @@ class Spec(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_longlong), ("max_active", ctypes.c_int),
-                ("chunk_steps", ctypes.c_int), ("order", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("chunk_steps", ctypes.c_int), ("order", ctypes.c_int), ("max_active_fp64", ctypes.c_int),
+                ("reserved", ctypes.c_int * 4)]
 
 
 class Job(ctypes.Structure):
@@ -380,8 +381,9 @@ class Ragged:
 class Server:
     """Continuous-batching simulation server on one GPU (am_server)."""
 
-    def __init__(self, hbm_budget_bytes=0, max_active=0, chunk_steps=0, order="arrival"):
-        cfg = ServerConfig(int(hbm_budget_bytes), int(max_active), int(chunk_steps), ORDER[order])
+    def __init__(self, hbm_budget_bytes=0, max_active=0, chunk_steps=0, order="arrival", max_active_fp64=0):
+        cfg = ServerConfig(int(hbm_budget_bytes), int(max_active), int(chunk_steps), ORDER[order],
+                           int(max_active_fp64))
         self.h = ctypes.c_void_p()
         _check(lib.am_server_create(ctypes.byref(cfg), ctypes.byref(self.h)), None, "am_server_create")
         self._jobs = {}
@@ -439,7 +441,7 @@ def footprint_bytes(params):
     return lib.am_footprint_bytes(ctypes.byref(params))
 
 
-COLUMN_SHAPES = ("wide", "narrow")
+COLUMN_SHAPES = ("wide", "narrow", "wide8")   # "wide8": wide tiles, radix-8 passes (FP32 only)
 
 
 def set_column_shape(precision, ny, shape):
@@ -456,11 +458,12 @@ def column_shape(precision, ny):
 
 
 def autotune(params, nsteps=20):
-    """Time both column-pass shapes for `params` on this GPU, keep the faster.
-    Returns (ms per step wide, ms per step narrow, chosen shape)."""
-    ms = np.zeros(2)
+    """Time every column-pass shape built for `params`' precision on this GPU
+    and keep the fastest.  Returns ({shape: ms per step}, chosen shape)."""
+    ms = np.zeros(len(COLUMN_SHAPES))
     _check(lib.am_autotune(ctypes.byref(params), int(nsteps), _dptr(ms)), None, "am_autotune")
-    return float(ms[0]), float(ms[1]), column_shape(params.precision, params.ny)
+    times = {name: float(t) for name, t in zip(COLUMN_SHAPES, ms) if t >= 0}
+    return times, column_shape(params.precision, params.ny)
 
 
 def make_params(nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None, dealias="reference",

@@ -375,7 +375,7 @@ static am_status step_impl(am_handle *h, int nsteps, double *energy, int *nan_st
 namespace af {
 
 namespace {
-// [fp64][log2 Ny]: 0 wide, 1 narrow; seeded with the measured rule
+// [fp64][log2 Ny]: 0 wide, 1 narrow, 2 wide radix 8; seeded with the measured rule
 std::atomic<int> g_colv[2][LOG_MAX + 1] = {
     {{1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {0}, {0}},
     {{1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {0}, {0}}};
@@ -383,7 +383,10 @@ static_assert(LOG_MAX == 12, "seed table covers log2 Ny = 0..12");
 }  // namespace
 
 int col_variant(bool fp64, int logny) { return g_colv[fp64 ? 1 : 0][logny].load(std::memory_order_relaxed); }
-void set_col_variant(bool fp64, int logny, int v) { g_colv[fp64 ? 1 : 0][logny].store(v ? 1 : 0); }
+void set_col_variant(bool fp64, int logny, int v) { g_colv[fp64 ? 1 : 0][logny].store(v); }
+
+// True if column-pass shape v is built for this precision (wide radix 8: FP32 only).
+bool col_variant_built(bool fp64, int v) { return v >= 0 && v < NCOLV && !(fp64 && v == 2); }
 
 }  // namespace af
 
@@ -649,9 +652,10 @@ am_status am_row_passes_async(am_handle *h, int reps)
 
 am_status am_set_column_shape(int precision, int ny, int shape)
 {
-    if (!is_pow2(ny) || ny < (1 << LOG_MIN) || ny > (1 << LOG_MAX) || (shape != 0 && shape != 1) ||
+    if (!is_pow2(ny) || ny < (1 << LOG_MIN) || ny > (1 << LOG_MAX) || shape < 0 || shape >= NCOLV ||
         (precision != AM_FP32 && precision != AM_FP64))
         return AM_ERR_ARG;
+    if (!col_variant_built(precision == AM_FP64, shape)) return AM_ERR_UNSUPPORTED;
     set_col_variant(precision == AM_FP64, ilog2(ny), shape);
     return AM_OK;
 }
@@ -664,7 +668,7 @@ int am_column_shape(int precision, int ny)
     return col_variant(precision == AM_FP64, ilog2(ny));
 }
 
-am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[2])
+am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[3])
 {
     if (!p || nsteps < 1) return AM_ERR_ARG;
     am_handle *h = nullptr;
@@ -684,7 +688,12 @@ am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[2])
     int bestv = h ? h->colv : 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (!st && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) st = AM_ERR_CUDA;
-    for (int v = 0; v < 2 && !st; v++) {
+    bool first = true;
+    for (int v = 0; v < NCOLV && !st; v++) {
+        if (!col_variant_built(h->fp64, v)) {
+            if (ms_per_step) ms_per_step[v] = -1;   // not built for this precision
+            continue;
+        }
         st = h->fp64 ? use_col_variant<double>(h, v) : use_col_variant<float>(h, v);
         if (!st) st = am_step(h, 2, nullptr, nullptr);   // warm-up, builds the graph
         if (st) break;
@@ -698,9 +707,10 @@ am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[2])
         if (st) break;
         const double per = (double)ms / nsteps;
         if (ms_per_step) ms_per_step[v] = per;
-        if (v == 0 || per < best) {
+        if (first || per < best) {
             best = per;
             bestv = v;
+            first = false;
         }
     }
     if (e0) cudaEventDestroy(e0);

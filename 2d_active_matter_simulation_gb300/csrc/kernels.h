@@ -41,12 +41,15 @@ AF_HD cpx<T> lintab_value(const LinCoef &c, int ny, int kx, int y)
 // CTAs of a step column-pass launch over ntp column tiles of W columns.
 inline int col_grid(const LaunchShape &s, int ntp, int W) { return (ntp * W + s.per_block - 1) / s.per_block; }
 
+// Column-pass launch shapes: 0 wide, 1 narrow, 2 wide radix 8 (FP32 only).
+constexpr int NCOLV = 3;
+
 template <typename T>
 struct KernelTable {
     void (*row[LOG_MAX + 1])(StepArgs<T>);
     LaunchShape row_shape[LOG_MAX + 1];
-    void (*col[LOG_MAX + 1][2][5])(StepArgs<T>);   // [log2 Ny][shape: 0 wide, 1 narrow][mode]
-    LaunchShape col_shape[LOG_MAX + 1][2];
+    void (*col[LOG_MAX + 1][NCOLV][5])(StepArgs<T>);   // [log2 Ny][shape][mode]; null: shape not built
+    LaunchShape col_shape[LOG_MAX + 1][NCOLV];
     void (*rowfwd[LOG_MAX + 1])(const T *, cpx<T> *, const cpx<T> *, int, int);
     LaunchShape rowfwd_shape[LOG_MAX + 1];
     void (*colfwd[LOG_MAX + 1])(const cpx<T> *, cpx<T> *, const cpx<T> *, int, int, int, int, int, int, int);
@@ -79,14 +82,16 @@ constexpr int BATCH_LOG_MAX = 10;
 
 struct BatchTable {
     void (*row[LOG_MAX + 1])(const StepArgs<float> *);
-    void (*col[LOG_MAX + 1][2][5])(const StepArgs<float> *);   // [log2 Ny][shape][mode]
+    void (*col[LOG_MAX + 1][NCOLV][5])(const StepArgs<float> *);   // [log2 Ny][shape][mode]
 };
 
-// Column-pass launch shape (0 wide, 1 narrow) used for new simulations of this
-// precision and log2 Ny: a process-wide table seeded with the measured rule
-// (narrow below Ny = 2048) and updated by am_autotune / am_set_column_shape.
+// Column-pass launch shape (0 wide, 1 narrow, 2 wide radix 8) used for new
+// simulations of this precision and log2 Ny: a process-wide table seeded with
+// the measured rule (narrow below Ny = 2048) and updated by am_autotune /
+// am_set_column_shape.
 int col_variant(bool fp64, int logny);
 void set_col_variant(bool fp64, int logny, int v);
+bool col_variant_built(bool fp64, int v);
 
 const BatchTable &kernels_batch_f32();
 void fill_batch_7_8(BatchTable &t);

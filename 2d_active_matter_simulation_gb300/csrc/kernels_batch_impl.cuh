@@ -15,13 +15,13 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
     RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
-template <typename T, int LOG, int MODE, int NARROW>
-__global__ void __launch_bounds__(ColPass<T, LOG, MODE, NARROW>::THREADS, ColPass<T, LOG, MODE, NARROW>::MINB)
+template <typename T, int LOG, int MODE, int VAR>
+__global__ void __launch_bounds__(ColPass<T, LOG, MODE, VAR>::THREADS, ColPass<T, LOG, MODE, VAR>::MINB)
     k_col_b(const StepArgs<T> *__restrict__ args)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const StepArgs<T> a = args[blockIdx.y];
-    ColPass<T, LOG, MODE, NARROW>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+    ColPass<T, LOG, MODE, VAR>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
 template <int LOG, int HI>
@@ -39,6 +39,11 @@ struct FillB {
         t.col[LOG][1][2] = k_col_b<float, LOG, 2, 1>;
         t.col[LOG][1][3] = k_col_b<float, LOG, 3, 1>;
         t.col[LOG][1][4] = k_col_b<float, LOG, 4, 1>;
+        t.col[LOG][2][0] = k_col_b<float, LOG, 0, 2>;
+        t.col[LOG][2][1] = k_col_b<float, LOG, 1, 2>;
+        t.col[LOG][2][2] = k_col_b<float, LOG, 2, 2>;
+        t.col[LOG][2][3] = k_col_b<float, LOG, 3, 2>;
+        t.col[LOG][2][4] = k_col_b<float, LOG, 4, 2>;
         if constexpr (LOG < HI) FillB<LOG + 1, HI>::run(t);
     }
 };

@@ -15,12 +15,12 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
     RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
-template <typename T, int LOG, int MODE, int NARROW>
-__global__ void __launch_bounds__(ColPass<T, LOG, MODE, NARROW>::THREADS, ColPass<T, LOG, MODE, NARROW>::MINB)
+template <typename T, int LOG, int MODE, int VAR>
+__global__ void __launch_bounds__(ColPass<T, LOG, MODE, VAR>::THREADS, ColPass<T, LOG, MODE, VAR>::MINB)
     k_col(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    ColPass<T, LOG, MODE, NARROW>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+    ColPass<T, LOG, MODE, VAR>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
 template <typename T, int LOG>
@@ -103,6 +103,7 @@ struct Fill {
         t.row_shape[LOG] = {RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::smem_bytes(), RowKernel<T, LOG>::ROWS};
         fill_col<0>(t);
         fill_col<1>(t);
+        if constexpr (sizeof(T) == 4) fill_col<2>(t);   // wide radix 8: FP32 only
         t.rowfwd[LOG] = k_rowfwd<T, LOG>;
         t.rowfwd_shape[LOG] = {RowFwd<T, LOG>::THREADS, RowFwd<T, LOG>::smem_bytes(), RowFwd<T, LOG>::ROWS};
         t.colfwd[LOG] = k_colfwd<T, LOG>;

@@ -8,7 +8,10 @@
 //
 //  * admission (thread "admit"): pending requests are admitted in arrival
 //    order (or shortest job first) while their device footprint fits the HBM
-//    budget and an active slot is free.  Admission creates the request's
+//    budget and an active slot is free.  FP64 requests (about 20 times the GPU
+//    time of an FP32 request of the same size) have a lane of their own: at
+//    most max_active_fp64 of them are active at once, and an FP64 request
+//    waiting for that lane does not hold back the FP32 requests behind it.  Admission creates the request's
 //    handle, builds its initial field (the seeded band-limited generator or
 //    the caller's state) and loads it.  Finished handles are destroyed on this
 //    thread too (stream-ordered frees: no wait for other requests' work).
@@ -97,6 +100,7 @@ struct am_server {
     long long next_id = 1;
     long long used = 0;                            // reserved device bytes
     int active = 0;                                // admitted and not yet reaped
+    int active_fp64 = 0;                           // of which FP64
     bool stop = false;
     long long gps_done = 0, jobs_done = 0, peak_used = 0;
     int peak_active = 0;
@@ -240,20 +244,28 @@ void admit_loop(am_server *s)
             }
             s->used -= j->footprint;
             s->active--;
+            if (j->spec.params.precision == AM_FP64) s->active_fp64--;
         }
         if (s->stop && s->pending.empty() && s->active == 0) return;
         // pick the next request that may be admitted
+        // (FP64 requests whose lane is full are passed over; the first request
+        // that may take a slot is then admitted only if its footprint fits,
+        // so a large request is not overtaken indefinitely by smaller ones)
         auto pick = s->pending.end();
         if (!s->pending.empty() && s->active < s->cfg.max_active) {
+            const bool lane64 = s->active_fp64 < s->cfg.max_active_fp64;
+            auto eligible = [&](const std::shared_ptr<Job> &j) {
+                return lane64 || j->spec.params.precision != AM_FP64;
+            };
             if (s->cfg.order == AM_ORDER_SHORTEST_FIRST) {
-                pick = std::min_element(s->pending.begin(), s->pending.end(),
-                                        [](const std::shared_ptr<Job> &a, const std::shared_ptr<Job> &b) {
-                                            return work_of(a->spec) < work_of(b->spec);
-                                        });
+                for (auto it = s->pending.begin(); it != s->pending.end(); ++it)
+                    if (eligible(*it) && (pick == s->pending.end() || work_of((*it)->spec) < work_of((*pick)->spec)))
+                        pick = it;
             } else {
-                pick = s->pending.begin();
+                pick = std::find_if(s->pending.begin(), s->pending.end(), eligible);
             }
-            if (s->used + (*pick)->footprint > s->cfg.hbm_budget_bytes && s->active > 0) pick = s->pending.end();
+            if (pick != s->pending.end() && s->used + (*pick)->footprint > s->cfg.hbm_budget_bytes && s->active > 0)
+                pick = s->pending.end();
         }
         if (pick == s->pending.end()) {
             s->cv_admit.wait(lk);
@@ -263,6 +275,7 @@ void admit_loop(am_server *s)
         s->pending.erase(pick);
         s->used += j->footprint;
         s->active++;
+        if (j->spec.params.precision == AM_FP64) s->active_fp64++;
         s->peak_used = std::max(s->peak_used, s->used);
         s->peak_active = std::max(s->peak_active, s->active);
         lk.unlock();
@@ -387,6 +400,8 @@ am_status am_server_create(const am_server_config *cfg, am_server **out)
     if (cfg) c = *cfg;
     if (c.hbm_budget_bytes <= 0) c.hbm_budget_bytes = 180LL << 30;
     if (c.max_active <= 0) c.max_active = 16;
+    if (c.max_active_fp64 <= 0) c.max_active_fp64 = (c.max_active + 3) / 4;
+    if (c.max_active_fp64 > c.max_active) c.max_active_fp64 = c.max_active;
     if (c.chunk_steps <= 0) c.chunk_steps = 256;
     if (c.chunk_steps > af::handle_ring_capacity()) c.chunk_steps = af::handle_ring_capacity();
     if (c.order != AM_ORDER_ARRIVAL && c.order != AM_ORDER_SHORTEST_FIRST) return AM_ERR_ARG;

@@ -520,34 +520,43 @@ AF_HD void cp_async_wait_all()
 
 // --------------------------------------------------------------- column pass
 // CW adjacent kx columns per group of CW * TPC threads (lane c = column in the
-// group, j = thread of that column's transform), TILES groups per CTA.  Two
-// launch shapes, chosen per precision and Ny at run time (see col_variant):
-//  * wide (NARROW = 0): CW = W, a whole tile per group, so every store covers
+// group, j = thread of that column's transform), TILES groups per CTA.  Three
+// launch shapes (VAR), chosen per precision and Ny at run time (see
+// col_variant, am_autotune):
+//  * wide (VAR 0): CW = W, a whole tile per group, so every store covers
 //    whole 32-byte sectors (FP32 at Ny = 4096 takes half a tile, 512 threads,
-//    to stay within 128 registers).  Default for Ny >= 2048.
-//  * narrow (NARROW = 1): CW = 1, one column per group: CTAs of 128 threads
+//    to stay within 128 registers).  Radix 16 (FP32) / 8 (FP64).
+//  * narrow (VAR 1): CW = 1, one column per group: CTAs of 128 threads
 //    (FP32, Ny <= 2048), up to four per SM, each synchronising only its own
 //    warps.  Stores then cover a quarter sector each, which at 2048 cost more
 //    (ncu: 4x the L2 write sectors, 36 -> 47 us) than the extra CTAs won;
 //    below it the smaller CTAs win (ragged batch of 128^2..1024^2 grids
-//    +14%).  Default for Ny <= 1024.
+//    +14%).
+//  * wide radix 8 (VAR 2, FP32 only): whole tiles as VAR 0, but radix-8
+//    passes with twice the threads per column (8 values each, up to 1024
+//    threads per CTA, 64 registers): one more exchange per transform, twice
+//    the warps per SM to hide the latency of a pass that is latency-bound
+//    with one 512-thread CTA per SM.
 // MODE 0 starts from u0 (after set_state), MODE 1..4 is the RK stage.
 // Launch: blockDim = THREADS, gridDim = ceil(columns carried / COLS).
-template <typename T, int LOGNY, int MODE, int NARROW = (LOGNY < 11 ? 1 : 0)>
+template <typename T, int LOGNY, int MODE, int VAR = (LOGNY < 11 ? 1 : 0)>
 struct ColPass {
+    static constexpr bool NARROW = VAR == 1;
+    static constexpr int TMAX = VAR == 2 ? 1024 : 512;   // threads per CTA at most
     static constexpr int W = Tile<T>::W;
-    static constexpr int LOGR = sizeof(T) == 4 ? 4 : 3;
+    static constexpr int LOGR = sizeof(T) == 4 && VAR != 2 ? 4 : 3;
     using FFTf = BlockFFT<T, LOGNY, LOGR, -1>;
     using FFTi = BlockFFT<T, LOGNY, LOGR, +1>;
     static constexpr int R = FFTf::R;
     static constexpr int TPC = FFTf::TPC;
     static constexpr int L = 1 << LOGNY;
-    static constexpr int CW = NARROW ? 1 : (W * TPC <= 512 ? W : (512 / TPC > 1 ? 512 / TPC : 1));
+    static constexpr int CW = NARROW ? 1 : (W * TPC <= TMAX ? W : (TMAX / TPC > 1 ? TMAX / TPC : 1));
     static constexpr int TILES = CW * TPC >= 128 ? 1 : 128 / (CW * TPC);   // column groups per CTA
     static constexpr int THREADS = TILES * CW * TPC;
     static constexpr int COLS = TILES * CW;                                // columns per CTA
-    // CTAs per SM the registers allow (128 per thread at most)
-    static constexpr int MINB = THREADS >= 512 ? 1 : (512 / THREADS > 4 ? 4 : 512 / THREADS);
+    // CTAs per SM the registers allow (128 per thread at most; VAR 2: 64)
+    static constexpr int MCAP = VAR == 2 ? 8 : 4;
+    static constexpr int MINB = THREADS >= TMAX ? 1 : (TMAX / THREADS > MCAP ? MCAP : TMAX / THREADS);
     // exchange slots: CW columns interleaved, idx + idx/8; one column: idx +
     // idx/16 (FP32) / idx + idx/8 (FP64), conflict-free for every pass of
     // these transforms (simulated bank pattern)

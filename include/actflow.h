@@ -229,7 +229,10 @@ typedef struct am_server_config {
     int chunk_steps;             /* largest chunk of steps (0: 256; at most 4096); each request's
                                     chunks hold about 20 ms of estimated GPU time, up to this */
     int order;                   /* am_order: admission order of pending requests */
-    int reserved[5];             /* must be zero */
+    int max_active_fp64;         /* FP64 requests on the GPU at once (0: max_active / 4, rounded up);
+                                    an FP64 request waiting for this lane does not hold back
+                                    the FP32 requests behind it */
+    int reserved[4];             /* must be zero */
 } am_server_config;
 
 typedef struct am_job {
@@ -280,21 +283,25 @@ am_status am_server_destroy(am_server *s);
 long long am_footprint_bytes(const am_params *p);
 
 /* ------------------------------------------------------ launch shapes --
- * The column pass has two launch shapes: 0 "wide" (a whole tile of adjacent
- * kx columns per group of threads, whole-sector stores, 512-thread CTAs) and
- * 1 "narrow" (one column per group, 128-thread CTAs, up to four per SM).
- * Which is faster depends on Ny and the precision; the process keeps one
- * choice per (precision, Ny), seeded with the rule measured on GB300 (narrow
- * below Ny = 2048), used by every handle, batch and ragged batch created
- * afterwards.  The reference has no counterpart (cuFFT picks its own plans,
- * ActFlow_V3-2.cu:507-508). */
+ * The column pass has three launch shapes: 0 "wide" (a whole tile of
+ * adjacent kx columns per group of threads, whole-sector stores, 512-thread
+ * CTAs, radix 16 in FP32), 1 "narrow" (one column per group, 128-thread CTAs,
+ * up to four per SM) and 2 "wide8" (FP32 only: wide tiles with radix-8
+ * passes, twice the threads per column, up to 1024-thread CTAs).  Which is
+ * fastest depends on Ny and the precision; the process keeps one choice per
+ * (precision, Ny), seeded with the rule measured on GB300 (narrow below
+ * Ny = 2048, wide above), used by every handle, batch and ragged batch
+ * created afterwards.  am_set_column_shape returns AM_ERR_UNSUPPORTED for a
+ * shape not built for the precision.  The reference has no counterpart
+ * (cuFFT picks its own plans, ActFlow_V3-2.cu:507-508). */
 am_status am_set_column_shape(int precision, int ny, int shape);
 int am_column_shape(int precision, int ny);   /* -1 for an unsupported size */
 /* Autotune: time nsteps steps of a simulation with parameters p under each
- * shape on the current device (a temporary handle with a seeded band-limited
- * state), store the faster one for p's precision and Ny, and report both
- * times in ms_per_step[2] (may be NULL). */
-am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[2]);
+ * shape built for its precision on the current device (a temporary handle with
+ * a seeded band-limited state), store the fastest for p's precision and Ny,
+ * and report the times in ms_per_step[3] (may be NULL; -1 for a shape not
+ * built for the precision). */
+am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[3]);
 
 /* Number of kernel launches one step makes (for accounting). */
 int am_launches_per_step(const am_handle *h);

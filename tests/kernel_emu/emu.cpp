@@ -38,7 +38,7 @@ void launch(int grid, int threads, size_t smem, Body body)
 
 template <typename T, int LX, int LY>
 struct Runner {
-    static int run(const am_params &p, T *w_hat, double *mean, int nsteps, double *energy)
+    static int run(const am_params &p, T *w_hat, double *mean, int nsteps, double *energy, int colvar)
     {
         HostTables<T> t;
         StepArgs<T> a{};
@@ -74,11 +74,20 @@ struct Runner {
         sc.m_new[1] = mean[1];
         sc.nan_step = -1;
         using RP = RowKernel<T, LX>;
+        // column-pass launch shape: the build's default for this length, or
+        // the one asked for (0 wide, 1 narrow, 2 wide radix 8 in FP32)
+        const int var = colvar < 0 || (colvar == 2 && sizeof(T) == 8) ? (LY < 11 ? 1 : 0) : colvar;
         auto col = [&](int mode) {
             auto go = [&](auto tag) {
-                using CP = ColPass<T, LY, decltype(tag)::value>;
-                launch((a.ntp * Tile<T>::W + CP::COLS - 1) / CP::COLS, CP::THREADS, CP::smem_bytes(),
-                       [&](int tid, int bid, unsigned char *sm, auto &sync) { CP::body(a, tid, bid, sm, sync); });
+                constexpr int MODE = decltype(tag)::value;
+                auto launch_var = [&](auto vtag) {
+                    using CP = ColPass<T, LY, MODE, decltype(vtag)::value>;
+                    launch((a.ntp * Tile<T>::W + CP::COLS - 1) / CP::COLS, CP::THREADS, CP::smem_bytes(),
+                           [&](int tid, int bid, unsigned char *sm, auto &sync) { CP::body(a, tid, bid, sm, sync); });
+                };
+                if (var == 0) launch_var(std::integral_constant<int, 0>{});
+                else if (var == 1) launch_var(std::integral_constant<int, 1>{});
+                else launch_var(std::integral_constant<int, 2>{});
             };
             switch (mode) {
             case 0: go(std::integral_constant<int, 0>{}); break;
@@ -142,6 +151,8 @@ struct Runner {
     }
 };
 
+int g_colvar = -1;   // column-pass shape asked for by emu_run (-1: the default)
+
 template <typename T, int LX, int LY>
 int dispatch_y(const am_params &p, T *w, double *m, int n, double *e, const T *real, int fwd, int mask)
 {
@@ -149,7 +160,7 @@ int dispatch_y(const am_params &p, T *w, double *m, int n, double *e, const T *r
         Runner<T, LX, LY>::forward(p, real, w, mask);
         return 0;
     }
-    return Runner<T, LX, LY>::run(p, w, m, n, e);
+    return Runner<T, LX, LY>::run(p, w, m, n, e, g_colvar);
 }
 
 template <typename T, int LX>
@@ -207,11 +218,13 @@ int dispatch(const am_params &p, T *w, double *m, int n, double *e, const T *rea
 }  // namespace
 
 extern "C" {
-// Advance (w_hat [ny][nx/2+1] complex of the precision, mean[2]) nsteps steps.
+// Advance (w_hat [ny][nx/2+1] complex of the precision, mean[2]) nsteps steps
+// with column-pass shape colvar (-1: the default for the length).
 // Returns the first NaN step or -1; -100 for an unsupported size (8..128 each,
 // or one side 512..4096 with the other 8..16).
-int emu_run(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy)
+int emu_run(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy, int colvar)
 {
+    g_colvar = colvar;
     if (p->precision == AM_FP64)
         return dispatch<double>(*p, (double *)w_hat, mean, nsteps, energy, nullptr, 0, 0);
     return dispatch<float>(*p, (float *)w_hat, mean, nsteps, energy, nullptr, 0, 0);

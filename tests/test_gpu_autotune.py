@@ -23,18 +23,29 @@ def _run(am, nx, ny, prec, shape, nsteps=4):
 
 
 @pytest.mark.parametrize("nx,ny,prec", [(256, 256, "fp32"), (2048, 2048, "fp32"), (128, 512, "fp64"),
-                                        (64, 4096, "fp32"), (64, 2048, "fp64")])
+                                        (64, 4096, "fp32"), (64, 2048, "fp64"), (128, 1024, "fp32"),
+                                        (32, 128, "fp32")])
 def test_column_shapes_agree(am, nx, ny, prec):
+    """Every candidate the autotuner may pick gives the same step: 1e-6 in FP32
+    (different radices round differently), 1e-12 in FP64."""
     old = am.column_shape(prec, ny)
+    shapes = ["wide", "narrow"] + (["wide8"] if prec == "fp32" else [])
     try:
-        ww, mw, ew = _run(am, nx, ny, prec, "wide")
-        wn, mn, en = _run(am, nx, ny, prec, "narrow")
+        res = {s: _run(am, nx, ny, prec, s) for s in shapes}
     finally:
         am.set_column_shape(prec, ny, old)
     tol = 1e-12 if prec == "fp64" else 1e-6
-    assert np.linalg.norm(ww - wn) / np.linalg.norm(ww) < tol
-    assert np.abs(ew - en).max() <= tol * np.abs(ew).max()
-    assert np.abs(mw - mn).max() <= tol * np.abs(mw).max()
+    ww, mw, ew = res["wide"]
+    for s in shapes[1:]:
+        wn, mn, en = res[s]
+        assert np.linalg.norm(ww - wn) / np.linalg.norm(ww) < tol, s
+        assert np.abs(ew - en).max() <= tol * np.abs(ew).max(), s
+        assert np.abs(mw - mn).max() <= tol * np.abs(mw).max(), s
+
+
+def test_fp64_has_no_radix8_shape(am):
+    with pytest.raises(am.ActflowError):
+        am.set_column_shape("fp64", 2048, "wide8")
 
 
 def test_autotune_keeps_the_faster_shape(am):
@@ -42,9 +53,9 @@ def test_autotune_keeps_the_faster_shape(am):
                        dealias="half")
     old = am.column_shape("fp32", 512)
     try:
-        wide, narrow, chosen = am.autotune(p, nsteps=10)
-        assert wide > 0 and narrow > 0
-        assert chosen == ("wide" if wide < narrow else "narrow")
+        times, chosen = am.autotune(p, nsteps=10)
+        assert set(times) == {"wide", "narrow", "wide8"} and min(times.values()) > 0
+        assert chosen == min(times, key=times.get)
         # a batch created now uses the chosen shape and still matches a lone handle
         b = am.Batch([p, p])
         w0 = am.ic_bandlimited(512, 512, 5, rms=0.5).astype(np.complex64)

@@ -79,3 +79,25 @@ def test_batch_rejects_mismatched_grids(am):
     p2 = am.make_params(256, 256, 1.0, 1.0, 0.01, 1.0, -0.8, 0.01)
     with pytest.raises(am.ActflowError):
         am.Batch([p1, p2])
+
+
+@pytest.mark.parametrize("dealias", ["half", "reference"])
+def test_batch_members_against_oracle(am, orc, dealias):
+    """The batched kernels (blockIdx.y = member) checked directly against the
+    oracle, not only against lone handles: each member of a 256^2 ensemble with
+    its own lambda and alpha, 20 steps, FP32 against the FP64 oracle (2e-5, the
+    short-horizon bound of the parity tests)."""
+    n, nb = 256, 3
+    mem = _members(am, n, nb, dealias, seed0=41)
+    batch = am.Batch([p for p, _, _ in mem])
+    for i, (_, w0, m0) in enumerate(mem):
+        batch.set_state(i, w0, m0)
+    e = batch.step(20)
+    for i, (p, w0, m0) in enumerate(mem):
+        wb, mb = batch.get_state(i)
+        op = orc.make_params(n, n, p.lx, p.ly, p.dt, p.lam, p.alpha, p.beta, p.gamma0, p.gamma2, dealias=dealias)
+        wo, mo, eo = orc.run(op, w0.astype(np.complex128), m0, 20, "f64")
+        assert np.linalg.norm(wb - wo) / np.linalg.norm(wo) < 2e-5, i
+        assert np.abs(mb - mo).max() <= 2e-5 * np.abs(mo).max(), i
+        assert np.abs(e[:, i] - eo).max() <= 2e-5 * np.abs(eo).max(), i
+    batch.close()

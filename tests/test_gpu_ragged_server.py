@@ -62,6 +62,34 @@ def test_ragged_runs_equal_solo_runs(am):
     r.close()
 
 
+def test_ragged_runs_against_oracle(am, orc):
+    """The batched kernels of a ragged batch checked directly against the
+    oracle: one run of each of three size classes (256^2, 128^2, 256x128), each
+    with its own parameters, dt and step count, FP32 against the FP64 oracle
+    (2e-5, the short-horizon bound of the parity tests)."""
+    rng = np.random.default_rng(11)
+    shapes = [(256, 256), (128, 128), (256, 128)]
+    steps = [15, 20, 10]
+    params = [_run_params(am, nx, ny, rng) for nx, ny in shapes]
+    r = am.Ragged(params, steps)
+    ics = []
+    for i, p in enumerate(params):
+        w0 = am.ic_bandlimited(p.nx, p.ny, 3000 + i, rms=0.5).astype(np.complex64)
+        m0 = (0.02 * p.nx * p.ny, 0.01 * (i + 1) * p.nx * p.ny)
+        ics.append((w0, m0))
+        r.set_state(i, w0, m0)
+    energies, _ = r.run()
+    for i, p in enumerate(params):
+        wr, mr = r.get_state(i)
+        op = orc.make_params(p.nx, p.ny, p.lx, p.ly, p.dt, p.lam, p.alpha, p.beta, p.gamma0, p.gamma2,
+                             dealias="half")
+        wo, mo, eo = orc.run(op, ics[i][0].astype(np.complex128), ics[i][1], steps[i], "f64")
+        assert np.linalg.norm(wr - wo) / np.linalg.norm(wo) < 2e-5, i
+        assert np.abs(mr - mo).max() <= 2e-5 * np.abs(mo).max(), i
+        assert np.abs(energies[i] - eo).max() <= 2e-5 * np.abs(eo).max(), i
+    r.close()
+
+
 def test_ragged_class_with_full_spectrum_run(am):
     """A run with modes outside the 1/2-rule ellipse makes its size class run
     the full transforms; every run still matches its lone handle."""
@@ -219,3 +247,29 @@ def test_server_small_request_overtakes_large_one(am):
     assert rs["status"] == am.AM_OK and rb["status"] == am.AM_OK
     assert rs["t_done"] < rb["t_done"]
     assert rs["t_admit"] < rb["t_done"]
+
+
+def test_server_fp64_lane(am):
+    """FP64 requests have a lane of their own: with one FP64 slot, the second
+    and third FP64 requests wait for the first to finish, while an FP32 request
+    submitted after them is admitted at once; every result is exact."""
+    p64 = am.make_params(512, 512, TWO_PI, TWO_PI, 1e-4, 3.5, -0.8, 0.01, gamma0=-0.045, gamma2=2.5e-5,
+                         dealias="half", precision="fp64")
+    p32 = am.make_params(256, 256, TWO_PI, TWO_PI, 1e-4, 3.5, -0.8, 0.01, gamma0=-0.045, gamma2=2.5e-5,
+                         dealias="half")
+    srv = am.Server(max_active=8, max_active_fp64=1, chunk_steps=32)
+    j64 = [srv.submit(p64, 300, seed=10 + i) for i in range(3)]
+    j32 = srv.submit(p32, 50, seed=20)
+    r64 = [srv.wait(j, timeout=300) for j in j64]
+    r32 = srv.wait(j32, timeout=300)
+    st = srv.stats()
+    srv.close()
+    assert all(r["status"] == am.AM_OK for r in r64) and r32["status"] == am.AM_OK
+    # one FP64 request at a time
+    assert r64[1]["t_admit"] >= r64[0]["t_done"] - 1e-3
+    assert r64[2]["t_admit"] >= r64[1]["t_done"] - 1e-3
+    # the FP32 request did not queue behind the waiting FP64 ones
+    assert r32["t_admit"] < r64[0]["t_done"]
+    assert st["peak_active"] <= 2
+    _check_against_solo(am, r32, p32, 50, 20, "fp32")
+    _check_against_solo(am, r64[2], p64, 300, 12, "fp64")

@@ -145,7 +145,9 @@ def _load():
         "am_footprint_bytes": ([ctypes.POINTER(Params)], ctypes.c_longlong),
         "am_set_column_shape": ([ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "am_column_shape": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
-        "am_autotune": ([ctypes.POINTER(Params), ctypes.c_int, dp], ctypes.c_int),
+        "am_autotune": ([ctypes.POINTER(Params), ctypes.c_int, dp, dp], ctypes.c_int),
+        "am_set_row_shape": ([ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "am_row_shape": ([ctypes.c_int, ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -167,7 +169,8 @@ EXPORTED = [
     "am_ragged_create", "am_ragged_destroy", "am_ragged_set_state", "am_ragged_get_state", "am_ragged_run",
     "am_ragged_device_bytes", "am_ragged_classes", "am_ragged_last_error",
     "am_server_create", "am_server_submit", "am_server_wait", "am_server_stats", "am_server_destroy",
-    "am_footprint_bytes", "am_set_column_shape", "am_column_shape", "am_autotune",
+    "am_footprint_bytes", "am_set_column_shape", "am_column_shape", "am_autotune", "am_set_row_shape",
+    "am_row_shape",
 ]
 
 
@@ -457,13 +460,32 @@ def column_shape(precision, ny):
     return COLUMN_SHAPES[v] if v >= 0 else None
 
 
+ROW_SHAPES = ("radix8", "radix16")   # "radix16": FP32, Nx >= 1024
+
+
+def set_row_shape(precision, nx, shape):
+    """Row-pass launch shape for new simulations of this precision and Nx."""
+    prec = FP64 if precision in ("fp64", FP64) else FP32
+    _check(lib.am_set_row_shape(prec, nx, ROW_SHAPES.index(shape) if isinstance(shape, str) else int(shape)),
+           None, "am_set_row_shape")
+
+
+def row_shape(precision, nx):
+    prec = FP64 if precision in ("fp64", FP64) else FP32
+    v = lib.am_row_shape(prec, nx)
+    return ROW_SHAPES[v] if v >= 0 else None
+
+
 def autotune(params, nsteps=20):
     """Time every column-pass shape built for `params`' precision on this GPU
-    and keep the fastest.  Returns ({shape: ms per step}, chosen shape)."""
-    ms = np.zeros(len(COLUMN_SHAPES))
-    _check(lib.am_autotune(ctypes.byref(params), int(nsteps), _dptr(ms)), None, "am_autotune")
-    times = {name: float(t) for name, t in zip(COLUMN_SHAPES, ms) if t >= 0}
-    return times, column_shape(params.precision, params.ny)
+    and keep the fastest, then every row-pass shape with it.  Returns
+    ({column shape: ms per step}, chosen column shape, {row shape: ms}, chosen row shape)."""
+    mc = np.zeros(len(COLUMN_SHAPES))
+    mr = np.zeros(len(ROW_SHAPES))
+    _check(lib.am_autotune(ctypes.byref(params), int(nsteps), _dptr(mc), _dptr(mr)), None, "am_autotune")
+    tc = {name: float(t) for name, t in zip(COLUMN_SHAPES, mc) if t >= 0}
+    tr = {name: float(t) for name, t in zip(ROW_SHAPES, mr) if t >= 0}
+    return tc, column_shape(params.precision, params.ny), tr, row_shape(params.precision, params.nx)
 
 
 def make_params(nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None, dealias="reference",

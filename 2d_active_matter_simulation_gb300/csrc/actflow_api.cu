@@ -45,7 +45,8 @@ int ilog2(int n)
 struct am_handle {
     am_params p{};
     int nxh = 0, nt = 0, W = 0, lognx = 0, logny = 0;
-    int colv = 0;                  // column-pass launch shape (0 wide, 1 narrow)
+    int colv = 0;                  // column-pass launch shape (0 wide, 1 narrow, 2 wide radix 8)
+    int rowv = 0;                  // row-pass launch shape (0 radix 8, 1 radix 16 with stashes)
     bool fp64 = false;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -161,7 +162,7 @@ static am_status alloc_and_tables(am_handle *h)
     struct {
         const void *fn;
         size_t smem;
-    } ks[] = {{(const void *)K.row[h->lognx], K.row_shape[h->lognx].smem},
+    } ks[] = {{(const void *)K.row[h->lognx][h->rowv], K.row_shape[h->lognx][h->rowv].smem},
               {(const void *)K.col[h->logny][h->colv][0], K.col_shape[h->logny][h->colv].smem},
               {(const void *)K.col[h->logny][h->colv][1], K.col_shape[h->logny][h->colv].smem},
               {(const void *)K.col[h->logny][h->colv][2], K.col_shape[h->logny][h->colv].smem},
@@ -193,9 +194,9 @@ template <typename T>
 static am_status launch_row(am_handle *h)
 {
     const KernelTable<T> &K = table<T>();
-    const LaunchShape &s = K.row_shape[h->lognx];
+    const LaunchShape &s = K.row_shape[h->lognx][h->rowv];
     int grid = (h->p.ny + s.per_block - 1) / s.per_block;
-    K.row[h->lognx]<<<grid, s.threads, s.smem, h->stream>>>(args_of<T>(h));
+    K.row[h->lognx][h->rowv]<<<grid, s.threads, s.smem, h->stream>>>(args_of<T>(h));
     CK(h, cudaGetLastError());
     return AM_OK;
 }
@@ -388,6 +389,19 @@ void set_col_variant(bool fp64, int logny, int v) { g_colv[fp64 ? 1 : 0][logny].
 // True if column-pass shape v is built for this precision (wide radix 8: FP32 only).
 bool col_variant_built(bool fp64, int v) { return v >= 0 && v < NCOLV && !(fp64 && v == 2); }
 
+namespace {
+// [fp64][log2 Nx]: 0 radix 8, 1 radix 16 with stashes; seeded with radix 8
+std::atomic<int> g_rowv[2][LOG_MAX + 1] = {};
+}  // namespace
+
+int row_variant(bool fp64, int lognx) { return g_rowv[fp64 ? 1 : 0][lognx].load(std::memory_order_relaxed); }
+void set_row_variant(bool fp64, int lognx, int v) { g_rowv[fp64 ? 1 : 0][lognx].store(v); }
+// Radix 16 with stashes: FP32, Nx >= 1024.
+bool row_variant_built(bool fp64, int lognx, int v)
+{
+    return v == 0 || (v == 1 && !fp64 && lognx >= ROWS_LOG_MIN && lognx <= LOG_MAX);
+}
+
 }  // namespace af
 
 // Switch a handle to column-pass shape v (kernel attributes, step graph).
@@ -405,6 +419,25 @@ static am_status use_col_variant(am_handle *h, int v)
         h->graph = nullptr;
     }
     h->colv = v;
+    return AM_OK;
+}
+
+// Switch a handle to row-pass shape v (kernel attribute, step graphs).
+template <typename T>
+static am_status use_row_variant(am_handle *h, int v)
+{
+    const KernelTable<T> &K = table<T>();
+    const LaunchShape &rs = K.row_shape[h->lognx][v];
+    if (rs.smem > 48 * 1024)
+        CK(h, cudaFuncSetAttribute((const void *)K.row[h->lognx][v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)rs.smem));
+    if (h->rowv != v) {
+        if (h->graph) cudaGraphExecDestroy(h->graph);
+        if (h->graph_rows) cudaGraphExecDestroy(h->graph_rows);
+        h->graph = nullptr;
+        h->graph_rows = nullptr;
+    }
+    h->rowv = v;
     return AM_OK;
 }
 
@@ -480,6 +513,7 @@ am_status am_create(const am_params *p, am_handle **out)
     h->lognx = ilog2(p->nx);
     h->logny = ilog2(p->ny);
     h->colv = col_variant(h->fp64, h->logny);
+    h->rowv = row_variant(h->fp64, h->lognx);
     cudaGetDevice(&h->device);
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete h;
@@ -668,7 +702,40 @@ int am_column_shape(int precision, int ny)
     return col_variant(precision == AM_FP64, ilog2(ny));
 }
 
-am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[3])
+am_status am_set_row_shape(int precision, int nx, int shape)
+{
+    if (!is_pow2(nx) || nx < (1 << LOG_MIN) || nx > (1 << LOG_MAX) || shape < 0 || shape >= NROWV ||
+        (precision != AM_FP32 && precision != AM_FP64))
+        return AM_ERR_ARG;
+    if (!row_variant_built(precision == AM_FP64, ilog2(nx), shape)) return AM_ERR_UNSUPPORTED;
+    set_row_variant(precision == AM_FP64, ilog2(nx), shape);
+    return AM_OK;
+}
+
+int am_row_shape(int precision, int nx)
+{
+    if (!is_pow2(nx) || nx < (1 << LOG_MIN) || nx > (1 << LOG_MAX) ||
+        (precision != AM_FP32 && precision != AM_FP64))
+        return -1;
+    return row_variant(precision == AM_FP64, ilog2(nx));
+}
+
+// Time nsteps graph replays of the handle's step (after two warm-up steps).
+static am_status time_steps(am_handle *h, int nsteps, cudaEvent_t e0, cudaEvent_t e1, double *per)
+{
+    am_status st = am_step(h, 2, nullptr, nullptr);   // warm-up, builds the graph
+    if (st) return st;
+    CK(h, cudaEventRecord(e0, h->stream));
+    for (int i = 0; i < nsteps; i++) CK(h, cudaGraphLaunch(h->graph, h->stream));
+    float ms = 0;
+    CK(h, cudaEventRecord(e1, h->stream));
+    CK(h, cudaEventSynchronize(e1));
+    CK(h, cudaEventElapsedTime(&ms, e0, e1));
+    *per = (double)ms / nsteps;
+    return AM_OK;
+}
+
+am_status am_autotune(const am_params *p, int nsteps, double ms_col[3], double ms_row[2])
 {
     if (!p || nsteps < 1) return AM_ERR_ARG;
     am_handle *h = nullptr;
@@ -684,39 +751,54 @@ am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[3])
         for (size_t i = 0; i < n; i++) wf[i] = (float)w[i];
     }
     if (!st) st = am_set_state(h, p->precision == AM_FP32 ? (const void *)wf.data() : (const void *)w.data(), nullptr);
-    double best = 0;
-    int bestv = h ? h->colv : 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (!st && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) st = AM_ERR_CUDA;
+    // Coordinate search: the column-pass shapes with the current row shape,
+    // then the row-pass shapes with the best column shape.
+    int bestc = h ? h->colv : 0, bestr = h ? h->rowv : 0;
+    double best = 0;
     bool first = true;
     for (int v = 0; v < NCOLV && !st; v++) {
         if (!col_variant_built(h->fp64, v)) {
-            if (ms_per_step) ms_per_step[v] = -1;   // not built for this precision
+            if (ms_col) ms_col[v] = -1;   // not built for this precision
             continue;
         }
         st = h->fp64 ? use_col_variant<double>(h, v) : use_col_variant<float>(h, v);
-        if (!st) st = am_step(h, 2, nullptr, nullptr);   // warm-up, builds the graph
+        double per = 0;
+        if (!st) st = time_steps(h, nsteps, e0, e1, &per);
         if (st) break;
-        if (cudaEventRecord(e0, h->stream) != cudaSuccess) st = AM_ERR_CUDA;
-        for (int i = 0; i < nsteps && !st; i++)
-            if (cudaGraphLaunch(h->graph, h->stream) != cudaSuccess) st = AM_ERR_CUDA;
-        float ms = 0;
-        if (!st && (cudaEventRecord(e1, h->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-                    cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
-            st = AM_ERR_CUDA;
-        if (st) break;
-        const double per = (double)ms / nsteps;
-        if (ms_per_step) ms_per_step[v] = per;
+        if (ms_col) ms_col[v] = per;
         if (first || per < best) {
             best = per;
-            bestv = v;
+            bestc = v;
+            first = false;
+        }
+    }
+    if (!st) st = h->fp64 ? use_col_variant<double>(h, bestc) : use_col_variant<float>(h, bestc);
+    first = true;
+    for (int v = 0; v < NROWV && !st; v++) {
+        if (!row_variant_built(h->fp64, h->lognx, v)) {
+            if (ms_row) ms_row[v] = -1;
+            continue;
+        }
+        st = h->fp64 ? use_row_variant<double>(h, v) : use_row_variant<float>(h, v);
+        double per = 0;
+        if (!st) st = time_steps(h, nsteps, e0, e1, &per);
+        if (st) break;
+        if (ms_row) ms_row[v] = per;
+        if (first || per < best) {
+            best = per;
+            bestr = v;
             first = false;
         }
     }
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     am_destroy(h);
-    if (!st) set_col_variant(p->precision == AM_FP64, ilog2(p->ny), bestv);
+    if (!st) {
+        set_col_variant(p->precision == AM_FP64, ilog2(p->ny), bestc);
+        set_row_variant(p->precision == AM_FP64, ilog2(p->nx), bestr);
+    }
     return st;
 }
 

@@ -32,7 +32,8 @@ constexpr int ECAP_B = 1024;   // energy ring entries per member
 struct am_batch {
     std::vector<am_params> p;
     int B = 0, nx = 0, ny = 0, nxh = 0, nt = 0, lognx = 0, logny = 0;
-    int colv = 0;                   // column-pass launch shape (0 wide, 1 narrow)
+    int colv = 0;                   // column-pass launch shape (0 wide, 1 narrow, 2 wide radix 8)
+    int rowv = 0;                   // row-pass launch shape (0 radix 8, 1 radix 16 with stashes)
     cudaStream_t stream = nullptr;
     size_t field_elems = 0;
     cpx<float> *fields = nullptr;   // [B][7][field]
@@ -92,14 +93,14 @@ am_status build_graph(am_batch *b)
     }
     const KernelTable<float> &K = kernels_f32();
     const BatchTable &KB = kernels_batch_f32();
-    const LaunchShape &rs = K.row_shape[b->lognx];
+    const LaunchShape &rs = K.row_shape[b->lognx][b->rowv];
     const LaunchShape &cs = K.col_shape[b->logny][b->colv];
     const dim3 rgrid((b->ny + rs.per_block - 1) / rs.per_block, b->B);
     const dim3 cgrid(col_grid(cs, ntp, Tile<float>::W), b->B);
     cudaGraph_t g;
     BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 1; s <= 4; s++) {
-        KB.row[b->lognx]<<<rgrid, rs.threads, rs.smem, b->stream>>>(b->dargs);
+        KB.row[b->lognx][b->rowv]<<<rgrid, rs.threads, rs.smem, b->stream>>>(b->dargs);
         KB.col[b->logny][b->colv][s]<<<cgrid, cs.threads, cs.smem, b->stream>>>(b->dargs);
     }
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
@@ -157,6 +158,7 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
     b->lognx = lx;
     b->logny = ly;
     b->colv = col_variant(false, ly);
+    b->rowv = row_variant(false, lx);
     b->loaded.assign(nmembers, 0);
     b->inside.assign(nmembers, 0);
     auto fail = [&](am_status s) {
@@ -219,9 +221,9 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
     // Large shared-memory opt-in for the batched kernels (same sizes as the single ones).
     const KernelTable<float> &K = kernels_f32();
     const BatchTable &KB = kernels_batch_f32();
-    const size_t rsm = K.row_shape[lx].smem, csm = K.col_shape[ly][b->colv].smem;
-    if (rsm > 48 * 1024 &&
-        cudaFuncSetAttribute((const void *)KB.row[lx], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm))
+    const size_t rsm = K.row_shape[lx][b->rowv].smem, csm = K.col_shape[ly][b->colv].smem;
+    if (rsm > 48 * 1024 && cudaFuncSetAttribute((const void *)KB.row[lx][b->rowv],
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm))
         return fail(AM_ERR_CUDA);
     for (int m = 0; m < 5; m++)
         if (csm > 48 * 1024 &&

@@ -43,11 +43,15 @@ inline int col_grid(const LaunchShape &s, int ntp, int W) { return (ntp * W + s.
 
 // Column-pass launch shapes: 0 wide, 1 narrow, 2 wide radix 8 (FP32 only).
 constexpr int NCOLV = 3;
+// Row-pass launch shapes: 0 radix 8 in lockstep (RowPass), 1 radix 16 with
+// stashes (RowPassS; FP32, Nx >= 512).
+constexpr int NROWV = 2;
+constexpr int ROWS_LOG_MIN = 10;   // RowPassS needs Nx >= 512 (log2 9); it is built from 1024 up
 
 template <typename T>
 struct KernelTable {
-    void (*row[LOG_MAX + 1])(StepArgs<T>);
-    LaunchShape row_shape[LOG_MAX + 1];
+    void (*row[LOG_MAX + 1][NROWV])(StepArgs<T>);   // [log2 Nx][shape]; null: shape not built
+    LaunchShape row_shape[LOG_MAX + 1][NROWV];
     void (*col[LOG_MAX + 1][NCOLV][5])(StepArgs<T>);   // [log2 Ny][shape][mode]; null: shape not built
     LaunchShape col_shape[LOG_MAX + 1][NCOLV];
     void (*rowfwd[LOG_MAX + 1])(const T *, cpx<T> *, const cpx<T> *, int, int);
@@ -81,7 +85,7 @@ constexpr int BATCH_LOG_MIN = 7;
 constexpr int BATCH_LOG_MAX = 10;
 
 struct BatchTable {
-    void (*row[LOG_MAX + 1])(const StepArgs<float> *);
+    void (*row[LOG_MAX + 1][NROWV])(const StepArgs<float> *);       // [log2 Nx][shape]
     void (*col[LOG_MAX + 1][NCOLV][5])(const StepArgs<float> *);   // [log2 Ny][shape][mode]
 };
 
@@ -92,6 +96,11 @@ struct BatchTable {
 int col_variant(bool fp64, int logny);
 void set_col_variant(bool fp64, int logny, int v);
 bool col_variant_built(bool fp64, int v);
+// Row-pass launch shape for new simulations of this precision and log2 Nx
+// (0 radix 8, 1 radix 16 with stashes), as col_variant.
+int row_variant(bool fp64, int lognx);
+void set_row_variant(bool fp64, int lognx, int v);
+bool row_variant_built(bool fp64, int lognx, int v);
 
 const BatchTable &kernels_batch_f32();
 void fill_batch_7_8(BatchTable &t);

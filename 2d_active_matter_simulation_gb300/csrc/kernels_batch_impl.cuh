@@ -15,6 +15,15 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
     RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
+template <typename T, int LOG>
+__global__ void __launch_bounds__(RowPassS<T, LOG>::THREADS, RowPassS<T, LOG>::MINB)
+    k_rows_b(const StepArgs<T> *__restrict__ args)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const StepArgs<T> a = args[blockIdx.y];
+    RowPassS<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+}
+
 template <typename T, int LOG, int MODE, int VAR>
 __global__ void __launch_bounds__(ColPass<T, LOG, MODE, VAR>::THREADS, ColPass<T, LOG, MODE, VAR>::MINB)
     k_col_b(const StepArgs<T> *__restrict__ args)
@@ -28,7 +37,8 @@ template <int LOG, int HI>
 struct FillB {
     static void run(BatchTable &t)
     {
-        t.row[LOG] = k_row_b<float, LOG>;
+        t.row[LOG][0] = k_row_b<float, LOG>;
+        if constexpr (LOG >= ROWS_LOG_MIN) t.row[LOG][1] = k_rows_b<float, LOG>;
         t.col[LOG][0][0] = k_col_b<float, LOG, 0, 0>;
         t.col[LOG][0][1] = k_col_b<float, LOG, 1, 0>;
         t.col[LOG][0][2] = k_col_b<float, LOG, 2, 0>;

@@ -15,6 +15,13 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
     RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
 }
 
+template <typename T, int LOG>
+__global__ void __launch_bounds__(RowPassS<T, LOG>::THREADS, RowPassS<T, LOG>::MINB) k_rows(StepArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    RowPassS<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); });
+}
+
 template <typename T, int LOG, int MODE, int VAR>
 __global__ void __launch_bounds__(ColPass<T, LOG, MODE, VAR>::THREADS, ColPass<T, LOG, MODE, VAR>::MINB)
     k_col(StepArgs<T> a)
@@ -99,8 +106,12 @@ struct Fill {
     }
     static void run(KernelTable<T> &t)
     {
-        t.row[LOG] = k_row<T, LOG>;
-        t.row_shape[LOG] = {RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::smem_bytes(), RowKernel<T, LOG>::ROWS};
+        t.row[LOG][0] = k_row<T, LOG>;
+        t.row_shape[LOG][0] = {RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::smem_bytes(), RowKernel<T, LOG>::ROWS};
+        if constexpr (sizeof(T) == 4 && LOG >= ROWS_LOG_MIN) {   // radix-16 row shape: FP32, Nx >= 1024
+            t.row[LOG][1] = k_rows<T, LOG>;
+            t.row_shape[LOG][1] = {RowPassS<T, LOG>::THREADS, RowPassS<T, LOG>::smem_bytes(), RowPassS<T, LOG>::ROWS};
+        }
         fill_col<0>(t);
         fill_col<1>(t);
         if constexpr (sizeof(T) == 4) fill_col<2>(t);   // wide radix 8: FP32 only

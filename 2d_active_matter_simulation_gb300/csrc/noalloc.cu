@@ -180,11 +180,12 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
     a.inv_2n3 = 1.0 / (2.0 * nd * nd * nd);
 
     const KernelTable<T> &K = table<T>();
-    const LaunchShape &rs = K.row_shape[lx2];
+    const int rowv = row_variant(sizeof(T) == 8, lx2);
+    const LaunchShape &rs = K.row_shape[lx2][rowv];
     const int colv = col_variant(sizeof(T) == 8, ly2);
     const LaunchShape &cs = K.col_shape[ly2][colv];
     if (rs.smem > 48 * 1024 &&
-        cudaFuncSetAttribute((const void *)K.row[lx2], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs.smem))
+        cudaFuncSetAttribute((const void *)K.row[lx2][rowv], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs.smem))
         return AM_ERR_CUDA;
     for (int m = 0; m < 5; m++)
         if (cs.smem > 48 * 1024 && cudaFuncSetAttribute((const void *)K.col[ly2][colv][m],
@@ -203,7 +204,7 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
     K.col[ly2][colv][0]<<<cgrid, cs.threads, cs.smem, st>>>(b);
     for (int n = 0; n < nsteps; n++) {
         for (int stage = 1; stage <= 4; stage++) {
-            K.row[lx2]<<<rgrid, rs.threads, rs.smem, st>>>(a);
+            K.row[lx2][rowv]<<<rgrid, rs.threads, rs.smem, st>>>(a);
             b.mode = stage;
             K.col[ly2][colv][stage]<<<cgrid, cs.threads, cs.smem, st>>>(b);
         }

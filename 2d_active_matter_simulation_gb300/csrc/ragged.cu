@@ -67,7 +67,8 @@ struct RaggedRun {
 
 struct SizeClass {
     int lognx = 0, logny = 0;
-    int colv = 0;               // column-pass launch shape (0 wide, 1 narrow)
+    int colv = 0;               // column-pass launch shape (0 wide, 1 narrow, 2 wide radix 8)
+    int rowv = 0;               // row-pass launch shape (0 radix 8, 1 radix 16 with stashes)
     std::vector<int> runs;      // run indices of this class
     std::vector<int> active;    // active runs (graph order)
     int ntp = 0;                // column tiles the passes touch (pruned or full)
@@ -181,7 +182,7 @@ am_status rebuild(am_ragged *r, const std::vector<char> &act)
         if (c.active.empty() || e != cudaSuccess) continue;
         e = cudaStreamWaitEvent(c.branch, r->fork, 0);
         if (e != cudaSuccess) break;
-        const LaunchShape &rs = K.row_shape[c.lognx];
+        const LaunchShape &rs = K.row_shape[c.lognx][c.rowv];
         const LaunchShape &cs = K.col_shape[c.logny][c.colv];
         const int ny = 1 << c.logny;
         const int nb = (int)c.active.size();
@@ -189,7 +190,7 @@ am_status rebuild(am_ragged *r, const std::vector<char> &act)
         const dim3 cgrid(col_grid(cs, c.ntp, Tile<float>::W), nb);
         const StepArgs<float> *args = r->dargs + c.off;
         for (int s = 1; s <= 4; s++) {
-            KB.row[c.lognx]<<<rgrid, rs.threads, rs.smem, c.branch>>>(args);
+            KB.row[c.lognx][c.rowv]<<<rgrid, rs.threads, rs.smem, c.branch>>>(args);
             KB.col[c.logny][c.colv][s]<<<cgrid, cs.threads, cs.smem, c.branch>>>(args);
         }
         e = cudaGetLastError();
@@ -258,6 +259,7 @@ am_status am_ragged_create(const am_params *params, const long long *nsteps, int
         r->cls[c].lognx = keys[c].first;
         r->cls[c].logny = keys[c].second;
         r->cls[c].colv = col_variant(false, keys[c].second);
+        r->cls[c].rowv = row_variant(false, keys[c].first);
     }
     size_t total = 0, stage = 0;
     for (int i = 0; i < nruns; i++) {
@@ -331,9 +333,9 @@ am_status am_ragged_create(const am_params *params, const long long *nsteps, int
     const KernelTable<float> &K = kernels_f32();
     const BatchTable &KB = kernels_batch_f32();
     for (const SizeClass &c : r->cls) {
-        const size_t rsm = K.row_shape[c.lognx].smem, csm = K.col_shape[c.logny][c.colv].smem;
-        if (rsm > 48 * 1024 &&
-            cudaFuncSetAttribute((const void *)KB.row[c.lognx], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm))
+        const size_t rsm = K.row_shape[c.lognx][c.rowv].smem, csm = K.col_shape[c.logny][c.colv].smem;
+        if (rsm > 48 * 1024 && cudaFuncSetAttribute((const void *)KB.row[c.lognx][c.rowv],
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm))
             return fail(AM_ERR_CUDA);
         for (int m = 0; m < 5; m++)
             if (csm > 48 * 1024 && cudaFuncSetAttribute((const void *)KB.col[c.logny][c.colv][m],

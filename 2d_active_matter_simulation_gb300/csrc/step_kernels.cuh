@@ -426,6 +426,203 @@ struct RowPass {
 template <typename T, int LOGNX>
 using RowKernel = RowPass<T, LOGNX>;
 
+// ----------------------------------------------- row pass, radix-16 shape
+// The same work as RowPass with radix-16 passes: TPC = M/16 threads per row
+// (64 at Nx = 2048), two exchanges per 1024-point transform instead of three,
+// and the transforms one after another instead of in lockstep: uy and ux,
+// once transformed, wait in two shared-memory stash buffers while w is
+// transformed (Q waits there while P is transformed), so each thread holds one
+// transform's 16 values at a time and the registers stay within 128.  Shared
+// memory per row: one exchange buffer (idx + idx/16 slots, the map of the
+// one-column radix-16 column pass) and the two stashes; the forward
+// transforms' pairing of Z(k) with Z(M-k) reads the stash that is free by
+// then.  FP32, Nx = 512 .. 4096.  Launch as RowPass.
+template <typename T, int LOGNX>
+struct RowPassS {
+    static constexpr int M = 1 << (LOGNX - 1);
+    static constexpr int LOGM = LOGNX - 1;
+    static constexpr int LOGR = 4;
+    using FFTi = BlockFFT<T, LOGM, LOGR, +1>;
+    using FFTf = BlockFFT<T, LOGM, LOGR, -1>;
+    static constexpr int R = FFTi::R;
+    static constexpr int TPC = FFTi::TPC;
+    static_assert(TPC >= 16 && TPC % Tile<T>::W == 0, "RowPassS: Nx >= 512");
+    static constexpr int ROWS = TPC >= 128 ? 1 : 128 / TPC;
+    static constexpr int THREADS = ROWS * TPC;
+    static constexpr int MINB = 4;
+    using Buf = XBuf<T, 1, 3>;
+    static constexpr int BUFS = (Buf::slots(M) + 7) / 8 * 8;
+    static constexpr int SLOTS = BUFS + 2 * M;    // exchange + two stashes (complex values)
+    static constexpr int NW = TPC / 32 > 0 ? TPC / 32 : 1;   // warps per row
+    static constexpr size_t smem_bytes()
+    {
+        return (size_t)ROWS * SLOTS * sizeof(cpx<T>) + (size_t)ROWS * 3 * 32 * sizeof(T);
+    }
+    using RP = RowPass<T, LOGNX>;
+
+    // X(k), X(M-k) for k = j + r TPC packed into Z(k) (as RowPass::pack_pairs;
+    // the twiddle of k is wj times a compile-time rotation by r / (2R) turns).
+    static AF_HD void load_pack(cpx<T> (&v)[R], const cpx<T> *src, int j, int y, int ny, int kxp, cpx<T> wj)
+    {
+        constexpr int W = Tile<T>::W;
+        const cpx<T> *pa = src + tidx<T>(j, y, ny);
+        const cpx<T> *pb = src + tidx<T>(M - j, y, ny);
+        const size_t stride = (size_t)(TPC / W) * ny * W;
+        static_for<0, R>([&](auto rc) {
+            constexpr int r = decltype(rc)::value;
+            const int k = j + r * TPC;
+            cpx<T> a = k <= kxp ? pa[r * stride] : mk<T>(0, 0);
+            cpx<T> b = M - k <= kxp ? pb[-(long long)(r * stride)] : mk<T>(0, 0);
+            b = conj(b);
+            if (r == 0 && j == 0) {   // X(0), X(M): imaginary parts dropped, as a half-plane C2R does
+                a.y = 0;
+                b.y = 0;
+            }
+            const cpx<T> Ev = a + b;
+            const cpx<T> O = rot<r, 2 * R, +1>(cmulc(a - b, wj));
+            v[r] = mk(Ev.x - O.y, Ev.y + O.x);
+        });
+    }
+
+    // R2C post-processing of the row's forward transform (v, cyclic) through
+    // the pairing buffer pb, stores of X(k) for k < kend.
+    template <class Sync>
+    static AF_HD void unpack_store(const cpx<T> (&v)[R], cpx<T> *pb, cpx<T> *dst, int j, int y, int ny, int kend,
+                                   bool active, cpx<T> wj, Sync &&sync)
+    {
+#pragma unroll
+        for (int r = 0; r < R; r++) pb[j + r * TPC] = v[r];
+        sync();
+        static_for<0, R>([&](auto rc) {
+            constexpr int r = decltype(rc)::value;
+            const int k = j + r * TPC;
+            if (active && k < kend) {
+                // X(k) = E + W^k O with W^k = wj exp(-2 pi i r / (2R))
+                const cpx<T> B = conj(pb[(M - k) & (M - 1)]);
+                const cpx<T> E = scale(v[r] + B, (T)0.5);
+                const cpx<T> D = scale(v[r] - B, (T)0.5);
+                dst[tidx<T>(k, y, ny)] = E + rot<r, 2 * R, -1>(cmul(mk(D.y, -D.x), wj));
+            }
+        });
+        if (active && j == 0 && M < kend) dst[tidx<T>(M, y, ny)] = RP::unpack(v[0], v[0], mk<T>(-1, 0));
+        for (int kx = M + 1 + j; active && kx < kend; kx += TPC) dst[tidx<T>(kx, y, ny)] = mk<T>(0, 0);
+    }
+
+    template <class Sync>
+    static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync)
+    {
+        static_assert(R == 16, "radix-16 shape");
+        const int rl = tid / TPC, j = tid % TPC;
+        const int yy = bid * ROWS + rl;
+        const bool active = yy < a.ny;
+        const int y = active ? yy : a.ny - 1;   // inactive rows recompute the last row, never store
+        const int ny = a.ny;
+        cpx<T> *base = reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * SLOTS;
+        const Buf xb{base};
+        cpx<T> *s1 = base + BUFS;   // uy, then Q, then Q^ for its pairing
+        cpx<T> *s2 = s1 + M;        // ux, then P^ for its pairing
+        T *scr = reinterpret_cast<T *>(reinterpret_cast<cpx<T> *>(smem) + (size_t)ROWS * SLOTS) + rl * 3 * 32;
+        const cpx<T> wj = ldtw(a.twx, j);
+
+        // ---- C2R along x of uy and ux (stashed), then w (kept in registers)
+        cpx<T> v[R];
+        load_pack(v, a.fy, j, y, ny, a.kxp, wj);
+        FFTi::run(v, j, 0, xb, a.twx, 2, sync);
+#pragma unroll
+        for (int r = 0; r < R; r++) s1[j + r * TPC] = v[r];
+        load_pack(v, a.fx, j, y, ny, a.kxp, wj);
+        FFTi::run(v, j, 0, xb, a.twx, 2, sync);
+#pragma unroll
+        for (int r = 0; r < R; r++) s2[j + r * TPC] = v[r];
+        load_pack(v, a.fa, j, y, ny, a.kxp, wj);
+        FFTi::run(v, j, 0, xb, a.twx, 2, sync);
+
+        // ---- real-space products (each thread reads and writes only its own
+        // stash slots): P to v, Q to s1
+        T se = 0, sx = 0, sy = 0;
+        const T lam = a.lam_s, bet = a.beta_s;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const cpx<T> uyv = s1[j + r * TPC], uxv = s2[j + r * TPC], wv = v[r];
+            const T ux0 = uxv.x, uy0 = uyv.x, w0 = wv.x, ux1 = uxv.y, uy1 = uyv.y, w1 = wv.y;
+            const T q0 = ux0 * ux0 + uy0 * uy0, q1 = ux1 * ux1 + uy1 * uy1;
+            se += q0 + q1;
+            sx += q0 * ux0 + q1 * ux1;
+            sy += q0 * uy0 + q1 * uy1;
+            v[r] = mk(lam * w0 * ux0 + bet * q0 * uy0, lam * w1 * ux1 + bet * q1 * uy1);
+            s1[j + r * TPC] = mk(lam * w0 * uy0 - bet * q0 * ux0, lam * w1 * uy1 - bet * q1 * ux1);
+        }
+        {
+            T t0 = se, t1 = sx, t2 = sy;
+            row_sum3(t0, t1, t2, j, scr, sync);
+            if (active && j == 0) {
+                a.rowp[y] = t0;
+                a.rowp[ny + y] = t1;
+                a.rowp[2 * ny + y] = t2;
+            }
+        }
+
+        // ---- R2C along x of P (pairing through s2, free since the products)
+        // and of Q (pairing through s1, which each thread has read back)
+        const int kend = a.ntp * Tile<T>::W;   // the column pass reads kx < kend
+        FFTf::run(v, j, 0, xb, a.twx, 2, sync);
+        unpack_store(v, s2, a.P, j, y, ny, kend, active, wj, sync);
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = s1[j + r * TPC];
+        FFTf::run(v, j, 0, xb, a.twx, 2, sync);   // its entry barrier orders the reads of s1 before the writes
+        unpack_store(v, s1, a.Q, j, y, ny, kend, active, wj, sync);
+    }
+
+    // Sum (t0, t1, t2) over the TPC threads of a row; valid in thread j = 0.
+    template <class Sync>
+    static AF_HD void row_sum3(T &t0, T &t1, T &t2, int j, T *scratch, Sync &&sync)
+    {
+#ifdef __CUDA_ARCH__
+        if constexpr (TPC >= 32) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+                t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+                t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+            }
+            if ((j & 31) == 0) {
+                scratch[(j >> 5) * 3 + 0] = t0;
+                scratch[(j >> 5) * 3 + 1] = t1;
+                scratch[(j >> 5) * 3 + 2] = t2;
+            }
+            sync();
+            if (j == 0) {
+                for (int w = 1; w < NW; w++) {
+                    t0 += scratch[w * 3 + 0];
+                    t1 += scratch[w * 3 + 1];
+                    t2 += scratch[w * 3 + 2];
+                }
+            }
+            return;
+        }
+#endif
+        // elsewhere (and for rows of fewer than 32 threads): thread 0 adds the
+        // row's values in thread order
+        for (int q = 0; q < TPC; q++) {
+            if (j == q) {
+                if (q == 0) {
+                    scratch[0] = t0;
+                    scratch[1] = t1;
+                    scratch[2] = t2;
+                } else {
+                    scratch[0] += t0;
+                    scratch[1] += t1;
+                    scratch[2] += t2;
+                }
+            }
+            sync();
+        }
+        t0 = scratch[0];
+        t1 = scratch[1];
+        t2 = scratch[2];
+    }
+};
+
 // ------------------------------------------------- sums over the row sums
 // Compensated ("float-float") accumulation for the FP32 path: hi + lo carries
 // about 44 significant bits, so the sum over all rows is as good as a double

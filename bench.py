@@ -410,7 +410,8 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if PRECISION == "fp32" else "f64", "data": "synthetic",
         "config": workload_config(),
         "timing": "CUDA events on the solver stream, one CUDA graph (8 kernels) per step",
-        "tuning": {"column_shape": tune[1], "autotune_ms_per_step": tune[0]},
+        "tuning": {"column_shape": tune[1], "autotune_ms_per_step": tune[0], "row_shape": tune[3],
+                   "autotune_row_ms_per_step": tune[2]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_source": traffic_src, "kernel": dom,
                      "algorithmic_bytes_per_launch": dom_bytes,
@@ -585,7 +586,8 @@ def run_batch(args):
         "config": {"workload": f"ensemble of {nb} x {NX}^2, FP32, dt={PARAMS['dt']:g}, 1/2 rule, one batch",
                    "members": nb, "timing": "host wall clock around am_batch_step (graph per step, energies "
                                             "of all members copied back per chunk)",
-                   "column_shape": tune[1], "autotune_ms_per_step": tune[0]},
+                   "column_shape": tune[1], "autotune_ms_per_step": tune[0], "row_shape": tune[3],
+                   "autotune_row_ms_per_step": tune[2]},
         "gpu_launches": 8 * args.steps, "clocks": clk,
     }
     print(json.dumps(out), flush=True)
@@ -618,7 +620,8 @@ def run_ragged(args):
     # column-pass launch shape per grid size, chosen by the autotuner on this GPU
     shapes = {}
     for n in sorted(set(sizes)):
-        shapes[f"{n}^2"] = am.autotune(params[sizes.index(n)], nsteps=10)[1]
+        t = am.autotune(params[sizes.index(n)], nsteps=10)
+        shapes[f"{n}^2"] = {"column": t[1], "row": t[3]}
     ics = [am.ic_bandlimited(n, n, 2000 + i).astype(np.complex64) for i, n in enumerate(sizes)]
     # warm-up: the same runs for `warmup` steps each
     warm = am.Ragged(params, [max(args.warmup, 1)] * nr)

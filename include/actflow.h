@@ -296,12 +296,23 @@ long long am_footprint_bytes(const am_params *p);
  * (cuFFT picks its own plans, ActFlow_V3-2.cu:507-508). */
 am_status am_set_column_shape(int precision, int ny, int shape);
 int am_column_shape(int precision, int ny);   /* -1 for an unsupported size */
-/* Autotune: time nsteps steps of a simulation with parameters p under each
- * shape built for its precision on the current device (a temporary handle with
- * a seeded band-limited state), store the fastest for p's precision and Ny,
- * and report the times in ms_per_step[3] (may be NULL; -1 for a shape not
- * built for the precision). */
-am_status am_autotune(const am_params *p, int nsteps, double ms_per_step[3]);
+/* The row pass has two launch shapes: 0 (radix-8 passes, 128 threads per
+ * 2048-point row, the three inverse transforms in lockstep) and 1 (FP32,
+ * Nx >= 1024: radix-16 passes, one exchange fewer per transform, half the
+ * threads per row, the transforms one after another with two shared-memory
+ * stashes).  One choice per (precision, Nx), seeded with shape 0, used by
+ * every handle, batch and ragged batch created afterwards; AM_ERR_UNSUPPORTED
+ * for a shape not built for the precision and Nx.  No counterpart in the
+ * reference. */
+am_status am_set_row_shape(int precision, int nx, int shape);
+int am_row_shape(int precision, int nx);      /* -1 for an unsupported size */
+/* Autotune: on the current device (a temporary handle with a seeded
+ * band-limited state), time nsteps steps of a simulation with parameters p
+ * under each column-pass shape built for its precision, keep the fastest for
+ * p's precision and Ny, then time each row-pass shape with that column shape
+ * and keep the fastest for p's precision and Nx.  The times go to ms_col[3]
+ * and ms_row[2] (either may be NULL; -1 for a shape not built). */
+am_status am_autotune(const am_params *p, int nsteps, double ms_col[3], double ms_row[2]);
 
 /* Number of kernel launches one step makes (for accounting). */
 int am_launches_per_step(const am_handle *h);

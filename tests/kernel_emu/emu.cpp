@@ -38,7 +38,7 @@ void launch(int grid, int threads, size_t smem, Body body)
 
 template <typename T, int LX, int LY>
 struct Runner {
-    static int run(const am_params &p, T *w_hat, double *mean, int nsteps, double *energy, int colvar)
+    static int run(const am_params &p, T *w_hat, double *mean, int nsteps, double *energy, int colvar, int rowvar)
     {
         HostTables<T> t;
         StepArgs<T> a{};
@@ -98,6 +98,14 @@ struct Runner {
             }
         };
         auto row = [&]() {
+            if constexpr (sizeof(T) == 4 && LX >= ROWS_LOG_MIN) {
+                if (rowvar == 1) {   // radix-16 row shape with stashes
+                    using RS = RowPassS<T, LX>;
+                    launch((ny + RS::ROWS - 1) / RS::ROWS, RS::THREADS, RS::smem_bytes(),
+                           [&](int tid, int bid, unsigned char *sm, auto &sync) { RS::body(a, tid, bid, sm, sync); });
+                    return;
+                }
+            }
             launch((ny + RP::ROWS - 1) / RP::ROWS, RP::THREADS, RP::smem_bytes(),
                    [&](int tid, int bid, unsigned char *sm, auto &sync) { RP::body(a, tid, bid, sm, sync); });
         };
@@ -152,6 +160,7 @@ struct Runner {
 };
 
 int g_colvar = -1;   // column-pass shape asked for by emu_run (-1: the default)
+int g_rowvar = 0;    // row-pass shape asked for by emu_run
 
 template <typename T, int LX, int LY>
 int dispatch_y(const am_params &p, T *w, double *m, int n, double *e, const T *real, int fwd, int mask)
@@ -160,7 +169,7 @@ int dispatch_y(const am_params &p, T *w, double *m, int n, double *e, const T *r
         Runner<T, LX, LY>::forward(p, real, w, mask);
         return 0;
     }
-    return Runner<T, LX, LY>::run(p, w, m, n, e, g_colvar);
+    return Runner<T, LX, LY>::run(p, w, m, n, e, g_colvar, g_rowvar);
 }
 
 template <typename T, int LX>
@@ -219,12 +228,14 @@ int dispatch(const am_params &p, T *w, double *m, int n, double *e, const T *rea
 
 extern "C" {
 // Advance (w_hat [ny][nx/2+1] complex of the precision, mean[2]) nsteps steps
-// with column-pass shape colvar (-1: the default for the length).
+// with column-pass shape colvar (-1: the default for the length) and row-pass
+// shape rowvar (0 radix 8, 1 radix 16 with stashes: FP32, Nx >= 1024).
 // Returns the first NaN step or -1; -100 for an unsupported size (8..128 each,
 // or one side 512..4096 with the other 8..16).
-int emu_run(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy, int colvar)
+int emu_run(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy, int colvar, int rowvar)
 {
     g_colvar = colvar;
+    g_rowvar = rowvar;
     if (p->precision == AM_FP64)
         return dispatch<double>(*p, (double *)w_hat, mean, nsteps, energy, nullptr, 0, 0);
     return dispatch<float>(*p, (float *)w_hat, mean, nsteps, energy, nullptr, 0, 0);

@@ -43,6 +43,34 @@ def test_column_shapes_agree(am, nx, ny, prec):
         assert np.abs(mw - mn).max() <= tol * np.abs(mw).max(), s
 
 
+@pytest.mark.parametrize("nx,ny", [(1024, 64), (2048, 2048), (4096, 32)])
+def test_row_shapes_agree(am, nx, ny):
+    """Both row-pass shapes give the same step (FP32, 1e-6)."""
+    old = am.row_shape("fp32", nx)
+    try:
+        am.set_row_shape("fp32", nx, "radix8")
+        w8, m8, e8 = _run(am, nx, ny, "fp32", am.column_shape("fp32", ny))
+        am.set_row_shape("fp32", nx, "radix16")
+        w16, m16, e16 = _run(am, nx, ny, "fp32", am.column_shape("fp32", ny))
+    finally:
+        am.set_row_shape("fp32", nx, old)
+    assert np.linalg.norm(w8 - w16) / np.linalg.norm(w8) < 1e-6
+    assert np.abs(e8 - e16).max() <= 1e-6 * np.abs(e8).max()
+    assert np.abs(m8 - m16).max() <= 1e-6 * np.abs(m8).max()
+
+
+def test_autotune_row_shape_at_2048(am):
+    p = am.make_params(2048, 256, 2 * math.pi, 2 * math.pi, 2e-4, 3.5, -0.8, 0.01, gamma0=-0.045,
+                       gamma2=2.5e-5, dealias="half")
+    oc, orr = am.column_shape("fp32", 256), am.row_shape("fp32", 2048)
+    try:
+        _, _, rtimes, rchosen = am.autotune(p, nsteps=5)
+        assert set(rtimes) == {"radix8", "radix16"} and rchosen == min(rtimes, key=rtimes.get)
+    finally:
+        am.set_column_shape("fp32", 256, oc)
+        am.set_row_shape("fp32", 2048, orr)
+
+
 def test_fp64_has_no_radix8_shape(am):
     with pytest.raises(am.ActflowError):
         am.set_column_shape("fp64", 2048, "wide8")
@@ -53,9 +81,10 @@ def test_autotune_keeps_the_faster_shape(am):
                        dealias="half")
     old = am.column_shape("fp32", 512)
     try:
-        times, chosen = am.autotune(p, nsteps=10)
+        times, chosen, rtimes, rchosen = am.autotune(p, nsteps=10)
         assert set(times) == {"wide", "narrow", "wide8"} and min(times.values()) > 0
         assert chosen == min(times, key=times.get)
+        assert set(rtimes) == {"radix8"} and rchosen == "radix8"   # radix 16 is built from Nx = 1024
         # a batch created now uses the chosen shape and still matches a lone handle
         b = am.Batch([p, p])
         w0 = am.ic_bandlimited(512, 512, 5, rms=0.5).astype(np.complex64)

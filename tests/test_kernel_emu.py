@@ -26,17 +26,17 @@ def emu(am):
                         "-I" + os.path.join(ROOT, "include"), "-I" + csrc, src, "-o", EMU_LIB], check=True)
     L = ctypes.CDLL(EMU_LIB)
     L.emu_run.argtypes = [ctypes.POINTER(am.Params), ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
-                          ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+                          ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_int]
     L.emu_forward.argtypes = [ctypes.POINTER(am.Params), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
     return L
 
 
-def _emu_run(am, emu, p, w0, mean0, n, colvar=-1):
+def _emu_run(am, emu, p, w0, mean0, n, colvar=-1, rowvar=0):
     w = np.ascontiguousarray(w0, dtype=np.complex128 if p.precision else np.complex64).copy()
     m = np.array(mean0, dtype=np.float64)
     e = np.zeros(max(n, 1))
     r = emu.emu_run(ctypes.byref(p), w.ctypes.data, m.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n,
-                    e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), colvar)
+                    e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), colvar, rowvar)
     assert r == -1
     return w, m, e[:n]
 
@@ -167,6 +167,24 @@ def test_emulated_radix8_column_shape(am, orc, emu, n, kind):
         w0 = w0 * orc.mask(nx, ny, "half")
     p = am.Params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, 0.0, 0.0, 0, am.DEALIAS["half"], 0)
     w, m, e = _emu_run(am, emu, p, w0, (3.0, 1.0), 3, colvar=2)
+    op = orc.make_params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, dealias="half", if_double=True)
+    wo, mo, eo = orc.run(op, w0, (3.0, 1.0), 3, "f64")
+    assert np.linalg.norm(w - wo) / np.linalg.norm(wo) < 2e-6
+    assert np.abs(m - mo).max() <= 2e-6 * np.abs(mo).max()
+    assert np.abs(e - eo).max() <= 2e-6 * np.abs(eo).max()
+
+
+@pytest.mark.parametrize("n,kind", [((2048, 8), "pruned"), ((1024, 8), "full"), ((4096, 8), "pruned")])
+def test_emulated_radix16_row_shape(am, orc, emu, n, kind):
+    """The second row-pass launch shape (radix-16 passes, transforms one after
+    another with shared-memory stashes), FP32, at the benchmark's row length and
+    at 1024 and 4096, against the FP64 oracle."""
+    nx, ny = n
+    w0 = np.fft.rfft2(np.random.default_rng(3 * nx + ny).standard_normal((ny, nx)))
+    if kind == "pruned":
+        w0 = w0 * orc.mask(nx, ny, "half")
+    p = am.Params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, 0.0, 0.0, 0, am.DEALIAS["half"], 0)
+    w, m, e = _emu_run(am, emu, p, w0, (3.0, 1.0), 3, rowvar=1)
     op = orc.make_params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, dealias="half", if_double=True)
     wo, mo, eo = orc.run(op, w0, (3.0, 1.0), 3, "f64")
     assert np.linalg.norm(w - wo) / np.linalg.norm(wo) < 2e-6

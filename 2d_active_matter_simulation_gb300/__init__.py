@@ -135,6 +135,7 @@ def _load():
         "am_ragged_run": ([hp, ctypes.POINTER(dp), ip, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
         "am_ragged_device_bytes": ([hp], ctypes.c_longlong),
         "am_ragged_classes": ([hp], ctypes.c_int),
+        "am_ragged_set_mode": ([hp, ctypes.c_int], ctypes.c_int),
         "am_ragged_last_error": ([hp], ctypes.c_char_p),
         "am_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(hp)], ctypes.c_int),
         "am_server_submit": ([hp, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
@@ -167,7 +168,7 @@ EXPORTED = [
     "am_read_snapshot", "am_append_energy", "am_cli_main", "am_batch_create", "am_batch_destroy",
     "am_batch_set_state", "am_batch_get_state", "am_batch_step", "am_batch_last_error",
     "am_ragged_create", "am_ragged_destroy", "am_ragged_set_state", "am_ragged_get_state", "am_ragged_run",
-    "am_ragged_device_bytes", "am_ragged_classes", "am_ragged_last_error",
+    "am_ragged_device_bytes", "am_ragged_classes", "am_ragged_set_mode", "am_ragged_last_error",
     "am_server_create", "am_server_submit", "am_server_wait", "am_server_stats", "am_server_destroy",
     "am_footprint_bytes", "am_set_column_shape", "am_column_shape", "am_autotune", "am_set_row_shape",
     "am_row_shape",
@@ -375,6 +376,10 @@ class Ragged:
     @property
     def classes(self):
         return lib.am_ragged_classes(self.h)
+
+    def set_mode(self, mode):
+        """"worklist" (one launch per pass for every size) or "per_class"."""
+        self._chk(lib.am_ragged_set_mode(self.h, {"worklist": 1, "per_class": 0}[mode]), "am_ragged_set_mode")
 
     @property
     def device_bytes(self):

@@ -28,7 +28,8 @@ CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 CUDA_UNITS = ["kernels_f32_12.cu", "kernels_f32_11.cu", "kernels_f64_12.cu", "kernels_f64_11.cu",
               "kernels_f32_10.cu", "kernels_batch_9_10.cu", "kernels_f32_3_6.cu", "kernels_f32_7_8.cu",
               "kernels_f32_9.cu", "kernels_f64_3_8.cu", "kernels_f64_9_10.cu",
-              "kernels_batch.cu", "kernels_f32.cu", "kernels_f64.cu", "actflow_api.cu", "noalloc.cu", "batch.cu",
+              "kernels_batch.cu", "kernels_queue.cu", "kernels_f32.cu", "kernels_f64.cu", "actflow_api.cu",
+              "noalloc.cu", "batch.cu",
               "ragged.cu", "server.cu"]
 HOST_UNITS = ["spec.cpp", "io.cpp", "driver.cpp", "cli.cpp"]
 

@@ -103,6 +103,23 @@ void set_row_variant(bool fp64, int lognx, int v);
 bool row_variant_built(bool fp64, int lognx, int v);
 
 const BatchTable &kernels_batch_f32();
+
+// Work-list kernels (kernels_queue.cu): one launch per pass over the runs of
+// several size classes.  Item = the run's argument index, the CTA index within
+// that run's own launch, log2 of the transform length (Nx for the row pass, Ny
+// for the column pass), 128..1024.  Row pass with radix-8 passes, narrow
+// column pass; CTAs of 128 threads.
+struct WorkItem {
+    int arg, block, log;
+};
+constexpr int QUEUE_LOG_MIN = 7;
+constexpr int QUEUE_LOG_MAX = 10;
+struct QueueTable {
+    void (*row)(const StepArgs<float> *, const WorkItem *);
+    void (*col[5])(const StepArgs<float> *, const WorkItem *);   // [mode], 1..4
+    size_t row_smem, col_smem;
+};
+const QueueTable &kernels_queue_f32();
 void fill_batch_7_8(BatchTable &t);
 void fill_batch_9_10(BatchTable &t);
 

@@ -10,6 +10,15 @@
 // CUDA graph whose classes are parallel branches (forked capture streams), so
 // the small grids' launches fill the SMs the large grids leave idle.
 //
+// Work-list mode (am_ragged_set_mode, the default): instead of one launch per
+// class, each pass of a stage is ONE launch over a work list of (run, CTA)
+// items of every class, sorted by grid size, largest first; each CTA runs the
+// kernel body of its item's length (kernels_queue.cu).  A step is then 8
+// launches whatever the number of classes, and the block scheduler hands out
+// the large grids' long items first.  It uses the radix-8 row pass and the
+// narrow column pass for every class (the shapes whose CTAs have 128 threads
+// at every length); the per-class mode uses each class's tuned shapes.
+//
 // Runs stop at their own step counts: the batch advances in segments of
 // k = min(remaining steps over the active runs, energy-ring capacity) steps;
 // after a segment the finished runs are dropped from the per-class argument
@@ -125,7 +134,11 @@ struct am_ragged {
     Scalars *sc_all = nullptr;        // scalars of every run, contiguous (reset kernel)
     double *ering_all = nullptr;      // energy rings [nruns][ECAP_R]
     StepArgs<float> *dargs = nullptr;
+    int mode = 1;                     // 1: one launch per pass over the work list; 0: per class
+    WorkItem *items = nullptr;        // device work lists: rows, then columns
+    size_t item_cap = 0;              // capacity of each list
     cudaGraphExec_t graph = nullptr;
+    int graph_mode = -1;
     std::vector<char> graph_set;      // active flags the graph was built for
     std::string err;
 };
@@ -141,11 +154,60 @@ struct am_ragged {
 
 namespace {
 
+// Work-list mode: the (run, CTA) items of every active run, classes largest
+// first (the order of r->cls), uploaded once per active set; the step graph is
+// the 8 work-list launches.  The arguments are already in dargs.
+am_status rebuild_worklist(am_ragged *r, const std::vector<char> &act, const KernelTable<float> &K)
+{
+    const QueueTable &Q = kernels_queue_f32();
+    std::vector<WorkItem> rows, cols;
+    for (const SizeClass &c : r->cls) {
+        const LaunchShape &rs = K.row_shape[c.lognx][0];
+        const LaunchShape &cs = K.col_shape[c.logny][1];
+        const int rblocks = ((1 << c.logny) + rs.per_block - 1) / rs.per_block;
+        const int cblocks = col_grid(cs, c.ntp, Tile<float>::W);
+        for (size_t q = 0; q < c.active.size(); q++) {
+            for (int b = 0; b < rblocks; b++) rows.push_back({c.off + (int)q, b, c.lognx});
+            for (int b = 0; b < cblocks; b++) cols.push_back({c.off + (int)q, b, c.logny});
+        }
+    }
+    if (rows.size() > r->item_cap || cols.size() > r->item_cap) {
+        r->err = "work list larger than its buffer";
+        return AM_ERR_ARG;
+    }
+    RK(cudaMemcpyAsync(r->items, rows.data(), rows.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, r->stream));
+    RK(cudaMemcpyAsync(r->items + r->item_cap, cols.data(), cols.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                       r->stream));
+    RK(cudaStreamSynchronize(r->stream));
+    cudaGraph_t g;
+    RK(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 1; s <= 4; s++) {
+        Q.row<<<(unsigned)rows.size(), 128, Q.row_smem, r->stream>>>(r->dargs, r->items);
+        Q.col[s]<<<(unsigned)cols.size(), 128, Q.col_smem, r->stream>>>(r->dargs, r->items + r->item_cap);
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaError_t e2 = cudaStreamEndCapture(r->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        r->err = std::string("capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2);
+        if (e2 == cudaSuccess) cudaGraphDestroy(g);
+        return AM_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&r->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        r->err = std::string("instantiate: ") + cudaGetErrorString(e);
+        return AM_ERR_CUDA;
+    }
+    r->graph_set = act;
+    r->graph_mode = 1;
+    return AM_OK;
+}
+
 // Upload the per-class argument arrays of the active runs and capture the
 // step graph: one branch per class, largest grids first.
 am_status rebuild(am_ragged *r, const std::vector<char> &act)
 {
-    if (r->graph && r->graph_set == act) return AM_OK;
+    if (r->graph && r->graph_set == act && r->graph_mode == r->mode) return AM_OK;
     if (r->graph) {
         cudaGraphExecDestroy(r->graph);
         r->graph = nullptr;
@@ -175,6 +237,7 @@ am_status rebuild(am_ragged *r, const std::vector<char> &act)
 
     const KernelTable<float> &K = kernels_f32();
     const BatchTable &KB = kernels_batch_f32();
+    if (r->mode == 1) return rebuild_worklist(r, act, K);
     cudaGraph_t g;
     RK(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaEventRecord(r->fork, r->stream);
@@ -210,6 +273,7 @@ am_status rebuild(am_ragged *r, const std::vector<char> &act)
         return AM_ERR_CUDA;
     }
     r->graph_set = act;
+    r->graph_mode = 0;
     return AM_OK;
 }
 
@@ -332,6 +396,27 @@ am_status am_ragged_create(const am_params *params, const long long *nsteps, int
     // Large shared-memory opt-in for every class's kernels.
     const KernelTable<float> &K = kernels_f32();
     const BatchTable &KB = kernels_batch_f32();
+    // Work lists (one per pass type) sized for every run at once, full transforms.
+    {
+        size_t cap = 0;
+        for (const RaggedRun &R : r->runs) {
+            const int lx = ilog2_exact(R.p.nx), ly = ilog2_exact(R.p.ny);
+            const LaunchShape &rs = K.row_shape[lx][0];
+            const LaunchShape &cs = K.col_shape[ly][1];
+            cap += (size_t)std::max((R.p.ny + rs.per_block - 1) / rs.per_block, col_grid(cs, R.nt, Tile<float>::W));
+        }
+        r->item_cap = cap;
+        if (cudaMalloc(&r->items, 2 * cap * sizeof(WorkItem)) != cudaSuccess) return fail(AM_ERR_OOM);
+        const QueueTable &Q = kernels_queue_f32();
+        if (Q.row_smem > 48 * 1024 && cudaFuncSetAttribute((const void *)Q.row, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                           (int)Q.row_smem) != cudaSuccess)
+            return fail(AM_ERR_CUDA);
+        for (int m = 1; m <= 4; m++)
+            if (Q.col_smem > 48 * 1024 && cudaFuncSetAttribute((const void *)Q.col[m],
+                                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                               (int)Q.col_smem) != cudaSuccess)
+                return fail(AM_ERR_CUDA);
+    }
     for (const SizeClass &c : r->cls) {
         const size_t rsm = K.row_shape[c.lognx][c.rowv].smem, csm = K.col_shape[c.logny][c.colv].smem;
         if (rsm > 48 * 1024 && cudaFuncSetAttribute((const void *)KB.row[c.lognx][c.rowv],
@@ -354,7 +439,7 @@ am_status am_ragged_destroy(am_ragged *r)
     if (!r) return AM_OK;
     if (r->stream) cudaStreamSynchronize(r->stream);
     if (r->graph) cudaGraphExecDestroy(r->graph);
-    void *ptrs[] = {r->pool, r->stage, r->sc_all, r->ering_all, r->dargs};
+    void *ptrs[] = {r->pool, r->stage, r->sc_all, r->ering_all, r->dargs, r->items};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     for (SizeClass &c : r->cls) {
@@ -479,11 +564,18 @@ long long am_ragged_device_bytes(const am_ragged *r)
     if (!r) return 0;
     size_t stage = 0;
     for (const RaggedRun &R : r->runs) stage = std::max(stage, (size_t)R.p.ny * R.nxh * sizeof(cpx<float>));
-    return (long long)(r->pool_bytes + stage +
+    return (long long)(r->pool_bytes + stage + 2 * r->item_cap * sizeof(WorkItem) +
                        r->runs.size() * (sizeof(Scalars) + ECAP_R * sizeof(double) + sizeof(StepArgs<float>)));
 }
 
 int am_ragged_classes(const am_ragged *r) { return r ? (int)r->cls.size() : 0; }
+
+am_status am_ragged_set_mode(am_ragged *r, int mode)
+{
+    if (!r || (mode != 0 && mode != 1)) return AM_ERR_ARG;
+    r->mode = mode;   // the next am_ragged_run rebuilds its graph
+    return AM_OK;
+}
 
 const char *am_ragged_last_error(const am_ragged *r) { return r ? r->err.c_str() : ""; }
 

@@ -35,12 +35,16 @@ def _solo(am, p, w0, m0, nsteps, precision="fp32"):
     return w, m, e
 
 
-def test_ragged_runs_equal_solo_runs(am):
+@pytest.mark.parametrize("mode", ["worklist", "per_class"])
+def test_ragged_runs_equal_solo_runs(am, mode):
+    """Every run equals a lone handle bit for bit, in both modes: one launch per
+    pass over the size-sorted work list, and one launch per size class."""
     rng = np.random.default_rng(3)
     shapes = [(128, 128), (256, 256), (128, 128), (512, 512), (256, 128), (1024, 1024), (256, 256)]
     steps = [7, 12, 3, 12, 5, 4, 9]
     params = [_run_params(am, nx, ny, rng) for nx, ny in shapes]
     r = am.Ragged(params, steps)
+    r.set_mode(mode)
     assert r.classes == 5
     ics = []
     for i, p in enumerate(params):

@@ -191,12 +191,12 @@ const char *am_batch_last_error(const am_batch *b);
  * time steps and step counts together.  The reference runs one simulation per
  * process (its time loop, ActFlow_V3-2.cu:718-862); a ragged batch is that loop
  * for R independent runs.  Runs are grouped by grid size, largest first.  In
- * the default work-list mode each pass of a step is ONE launch over a list of
- * (run, CTA) items of every active run, sorted by grid size, largest first
- * (8 launches per step whatever the sizes; radix-8 row and narrow column
- * passes for every size).  In per-class mode each pass is one launch per size
- * class (the class's tuned shapes), the classes running as parallel branches
- * of one CUDA graph per step.  A run stops at its own step count.  FP32, grids
+ * the default per-class mode each pass is one launch per size class (the
+ * class's tuned shapes), the classes running as parallel branches of one CUDA
+ * graph per step.  In work-list mode each pass of a step is ONE launch over a
+ * list of (run, CTA) items of every active run, sorted by grid size, largest
+ * first (8 launches per step whatever the sizes; radix-8 row and narrow
+ * column passes for every size).  A run stops at its own step count.  FP32, grids
  * 128..1024 per axis.  Each run computes exactly what a handle with its
  * parameters and the same launch shapes computes. */
 typedef struct am_ragged am_ragged;
@@ -213,8 +213,8 @@ am_status am_ragged_get_state(am_ragged *r, int run, void *w_hat, double mean[2]
 am_status am_ragged_run(am_ragged *r, double *const *energy, int *nan_run, long long *grid_point_steps);
 long long am_ragged_device_bytes(const am_ragged *r);
 int am_ragged_classes(const am_ragged *r);
-/* 1: one launch per pass over the work list (default); 0: one launch per
- * size class per pass.  Takes effect at the next am_ragged_run. */
+/* 0: one launch per size class per pass (default); 1: one launch per pass
+ * over the work list.  Takes effect at the next am_ragged_run. */
 am_status am_ragged_set_mode(am_ragged *r, int mode);
 const char *am_ragged_last_error(const am_ragged *r);
 

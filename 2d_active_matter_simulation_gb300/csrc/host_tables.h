@@ -158,16 +158,20 @@ void set_pruning(StepArgs<T> &a, bool on)
 
 // True if the half-plane state w ([ny][nxh] complex, interleaved) is zero at
 // every mode the 1/2 rule removes.
+// The kept modes of a row form a prefix ix <= lim(iy) (mask_at's condition is
+// monotone in ix), so each row's limit is found once and only the entries past
+// it are tested.
 template <typename T>
 bool state_inside_half_mask(const T *w, int nx, int ny)
 {
     const int nxh = nx / 2 + 1;
+    int lim = nxh - 1;   // kept ix of the row: 0..lim (lim = -1: none)
     for (int iy = 0; iy < ny; iy++) {
-        for (int ix = 0; ix < nxh; ix++) {
-            if (mask_at(1, 0, nx, ny, ix, iy)) continue;
-            size_t k = ((size_t)iy * nxh + ix) * 2;
-            if (w[k] != 0 || w[k + 1] != 0) return false;
-        }
+        while (lim >= 0 && !mask_at(1, 0, nx, ny, lim, iy)) lim--;
+        while (lim + 1 < nxh && mask_at(1, 0, nx, ny, lim + 1, iy)) lim++;
+        const T *row = w + (size_t)iy * nxh * 2;
+        for (int k = 2 * (lim + 1); k < 2 * nxh; k++)
+            if (row[k] != 0) return false;
     }
     return true;
 }

@@ -75,8 +75,8 @@ struct Runner {
         sc.nan_step = -1;
         using RP = RowKernel<T, LX>;
         // column-pass launch shape: the build's default for this length, or
-        // the one asked for (0 wide, 1 narrow, 2 wide radix 8 in FP32)
-        const int var = colvar < 0 || (colvar == 2 && sizeof(T) == 8) ? (LY < 11 ? 1 : 0) : colvar;
+        // the radix-8 shape (colvar 2, FP32)
+        const int var = colvar == 2 && sizeof(T) == 4 ? 2 : -1;
         auto col = [&](int mode) {
             auto go = [&](auto tag) {
                 constexpr int MODE = decltype(tag)::value;
@@ -85,9 +85,17 @@ struct Runner {
                     launch((a.ntp * Tile<T>::W + CP::COLS - 1) / CP::COLS, CP::THREADS, CP::smem_bytes(),
                            [&](int tid, int bid, unsigned char *sm, auto &sync) { CP::body(a, tid, bid, sm, sync); });
                 };
-                if (var == 0) launch_var(std::integral_constant<int, 0>{});
-                else if (var == 1) launch_var(std::integral_constant<int, 1>{});
-                else launch_var(std::integral_constant<int, 2>{});
+                // the default shape of the length, and the radix-8 shape at the
+                // column lengths its tests use (each instantiation adds to the
+                // harness's compile time)
+                constexpr int DEF = LY < 11 ? 1 : 0;
+                if constexpr (sizeof(T) == 4 && (LY == 7 || LY == 10 || LY == 11)) {
+                    if (var == 2) {
+                        launch_var(std::integral_constant<int, 2>{});
+                        return;
+                    }
+                }
+                launch_var(std::integral_constant<int, DEF>{});
             };
             switch (mode) {
             case 0: go(std::integral_constant<int, 0>{}); break;
@@ -159,92 +167,142 @@ struct Runner {
     }
 };
 
-int g_colvar = -1;   // column-pass shape asked for by emu_run (-1: the default)
-int g_rowvar = 0;    // row-pass shape asked for by emu_run
+// The harness compiles as several translation units in parallel (it is one
+// big template instantiation otherwise): with EMU_GROUP = g it instantiates
+// the row lengths of group g and exports emu_group_<g>; without it, it holds
+// the exported entry points, which call the group of the row length.
+constexpr int group_of(int lx) { return lx <= 5 ? 0 : lx <= 8 ? 1 : lx <= 10 ? 2 : lx == 11 ? 3 : 4; }
+constexpr int NGROUPS = 5;
 
+struct Call {
+    const am_params *p;
+    void *w;
+    double *m;
+    int n;
+    double *e;
+    const void *real;
+    int fwd, mask, colvar, rowvar;
+};
+
+#ifdef EMU_GROUP
 template <typename T, int LX, int LY>
-int dispatch_y(const am_params &p, T *w, double *m, int n, double *e, const T *real, int fwd, int mask)
+int dispatch_y(const Call &c)
 {
-    if (fwd) {
-        Runner<T, LX, LY>::forward(p, real, w, mask);
+    T *w = (T *)c.w;
+    if (c.fwd) {
+        Runner<T, LX, LY>::forward(*c.p, (const T *)c.real, w, c.mask);
         return 0;
     }
-    return Runner<T, LX, LY>::run(p, w, m, n, e, g_colvar, g_rowvar);
+    return Runner<T, LX, LY>::run(*c.p, w, c.m, c.n, c.e, c.colvar, c.rowvar);
 }
 
 template <typename T, int LX>
-int dispatch_x(int ly, const am_params &p, T *w, double *m, int n, double *e, const T *real, int fwd, int mask)
+int dispatch_x(int ly, const Call &c)
 {
-    switch (ly) {
-    case 3: return dispatch_y<T, LX, 3>(p, w, m, n, e, real, fwd, mask);
-    case 4: return dispatch_y<T, LX, 4>(p, w, m, n, e, real, fwd, mask);
-    case 5: return dispatch_y<T, LX, 5>(p, w, m, n, e, real, fwd, mask);
-    case 6: return dispatch_y<T, LX, 6>(p, w, m, n, e, real, fwd, mask);
-    case 7: return dispatch_y<T, LX, 7>(p, w, m, n, e, real, fwd, mask);
-    }
-    if constexpr (LX <= 4) {   // long columns with few of them: the column kernels at production lengths
+    if constexpr (LX <= 7) {
         switch (ly) {
-        case 9: return dispatch_y<T, LX, 9>(p, w, m, n, e, real, fwd, mask);
-        case 10: return dispatch_y<T, LX, 10>(p, w, m, n, e, real, fwd, mask);
-        case 11: return dispatch_y<T, LX, 11>(p, w, m, n, e, real, fwd, mask);
-        case 12: return dispatch_y<T, LX, 12>(p, w, m, n, e, real, fwd, mask);
+        case 3: return dispatch_y<T, LX, 3>(c);
+        case 4: return dispatch_y<T, LX, 4>(c);
+        case 5: return dispatch_y<T, LX, 5>(c);
+        case 6: return dispatch_y<T, LX, 6>(c);
+        case 7: return dispatch_y<T, LX, 7>(c);
+        }
+        if constexpr (LX <= 4) {   // long columns with few of them: the column kernels at production lengths
+            switch (ly) {
+            case 9: return dispatch_y<T, LX, 9>(c);
+            case 10: return dispatch_y<T, LX, 10>(c);
+            case 11: return dispatch_y<T, LX, 11>(c);
+            case 12: return dispatch_y<T, LX, 12>(c);
+            }
+        }
+    } else {   // long rows with few of them: the row kernels at production lengths
+        switch (ly) {
+        case 3: return dispatch_y<T, LX, 3>(c);
+        case 4: return dispatch_y<T, LX, 4>(c);
         }
     }
     return -100;
 }
 
-// Long rows with few of them: the row kernels at production lengths.
 template <typename T, int LX>
-int dispatch_long_x(int ly, const am_params &p, T *w, double *m, int n, double *e, const T *real, int fwd, int mask)
+int dispatch_if_group(int lx, int ly, const Call &c)
 {
-    switch (ly) {
-    case 3: return dispatch_y<T, LX, 3>(p, w, m, n, e, real, fwd, mask);
-    case 4: return dispatch_y<T, LX, 4>(p, w, m, n, e, real, fwd, mask);
+    if constexpr (group_of(LX) == EMU_GROUP) {
+        if (lx == LX) return dispatch_x<T, LX>(ly, c);
     }
-    return -100;
+    return -200;
 }
 
 template <typename T>
-int dispatch(const am_params &p, T *w, double *m, int n, double *e, const T *real, int fwd, int mask)
+int dispatch(int lx, int ly, const Call &c)
 {
-    int lx = 0, ly = 0;
-    while ((1 << lx) < p.nx) lx++;
-    while ((1 << ly) < p.ny) ly++;
-    switch (lx) {
-    case 3: return dispatch_x<T, 3>(ly, p, w, m, n, e, real, fwd, mask);
-    case 4: return dispatch_x<T, 4>(ly, p, w, m, n, e, real, fwd, mask);
-    case 5: return dispatch_x<T, 5>(ly, p, w, m, n, e, real, fwd, mask);
-    case 6: return dispatch_x<T, 6>(ly, p, w, m, n, e, real, fwd, mask);
-    case 7: return dispatch_x<T, 7>(ly, p, w, m, n, e, real, fwd, mask);
-    case 9: return dispatch_long_x<T, 9>(ly, p, w, m, n, e, real, fwd, mask);
-    case 10: return dispatch_long_x<T, 10>(ly, p, w, m, n, e, real, fwd, mask);
-    case 11: return dispatch_long_x<T, 11>(ly, p, w, m, n, e, real, fwd, mask);
-    case 12: return dispatch_long_x<T, 12>(ly, p, w, m, n, e, real, fwd, mask);
-    }
-    return -100;
+    int r = -100;
+    auto one = [&](int v) {
+        if (v != -200) r = v;
+    };
+    one(dispatch_if_group<T, 3>(lx, ly, c));
+    one(dispatch_if_group<T, 4>(lx, ly, c));
+    one(dispatch_if_group<T, 5>(lx, ly, c));
+    one(dispatch_if_group<T, 6>(lx, ly, c));
+    one(dispatch_if_group<T, 7>(lx, ly, c));
+    one(dispatch_if_group<T, 9>(lx, ly, c));
+    one(dispatch_if_group<T, 10>(lx, ly, c));
+    one(dispatch_if_group<T, 11>(lx, ly, c));
+    one(dispatch_if_group<T, 12>(lx, ly, c));
+    return r;
 }
+#endif
 
 }  // namespace
 
+#define EMU_CAT2(a, b) a##b
+#define EMU_CAT(a, b) EMU_CAT2(a, b)
+
 extern "C" {
+#ifdef EMU_GROUP
+int EMU_CAT(emu_group_, EMU_GROUP)(int lx, int ly, const Call *c)
+{
+    return c->p->precision == AM_FP64 ? dispatch<double>(lx, ly, *c) : dispatch<float>(lx, ly, *c);
+}
+#else
+int emu_group_0(int, int, const Call *);
+int emu_group_1(int, int, const Call *);
+int emu_group_2(int, int, const Call *);
+int emu_group_3(int, int, const Call *);
+int emu_group_4(int, int, const Call *);
+
+static int dispatch_all(const Call &c)
+{
+    int lx = 0, ly = 0;
+    while ((1 << lx) < c.p->nx) lx++;
+    while ((1 << ly) < c.p->ny) ly++;
+    int (*const groups[NGROUPS])(int, int, const Call *) = {emu_group_0, emu_group_1, emu_group_2, emu_group_3,
+                                                            emu_group_4};
+    return lx < 3 || lx > 12 ? -100 : groups[group_of(lx)](lx, ly, &c);
+}
+
 // Advance (w_hat [ny][nx/2+1] complex of the precision, mean[2]) nsteps steps
-// with column-pass shape colvar (-1: the default for the length) and row-pass
-// shape rowvar (0 radix 8, 1 radix 16 with stashes: FP32, Nx >= 1024).
+// with column-pass shape colvar (2: radix 8, FP32, column lengths 128, 1024,
+// 2048; otherwise the default for the length) and row-pass shape rowvar (0
+// radix 8, 1 radix 16 with stashes: FP32, Nx >= 1024).
 // Returns the first NaN step or -1; -100 for an unsupported size (8..128 each,
 // or one side 512..4096 with the other 8..16).
 int emu_run(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy, int colvar, int rowvar)
 {
-    g_colvar = colvar;
-    g_rowvar = rowvar;
-    if (p->precision == AM_FP64)
-        return dispatch<double>(*p, (double *)w_hat, mean, nsteps, energy, nullptr, 0, 0);
-    return dispatch<float>(*p, (float *)w_hat, mean, nsteps, energy, nullptr, 0, 0);
+    return dispatch_all(Call{p, w_hat, mean, nsteps, energy, nullptr, 0, 0, colvar, rowvar});
+}
+
+// The host check behind pruned transforms (host_tables.h): 1 if the half-plane
+// state is zero at every mode the 1/2 rule removes.
+int emu_inside_half(const am_params *p, const void *w_hat)
+{
+    if (p->precision == AM_FP64) return state_inside_half_mask<double>((const double *)w_hat, p->nx, p->ny) ? 1 : 0;
+    return state_inside_half_mask<float>((const float *)w_hat, p->nx, p->ny) ? 1 : 0;
 }
 
 int emu_forward(const am_params *p, const void *real, void *w_hat, int mask)
 {
-    if (p->precision == AM_FP64)
-        return dispatch<double>(*p, (double *)w_hat, nullptr, 0, nullptr, (const double *)real, 1, mask);
-    return dispatch<float>(*p, (float *)w_hat, nullptr, 0, nullptr, (const float *)real, 1, mask);
+    return dispatch_all(Call{p, w_hat, nullptr, 0, nullptr, real, 1, mask, -1, 0});
 }
+#endif
 }

@@ -21,13 +21,24 @@ def emu(am):
     csrc = os.path.join(ROOT, "2d_active_matter_simulation_gb300", "csrc")
     deps = [src] + [os.path.join(csrc, f) for f in os.listdir(csrc) if f.endswith((".cuh", ".h"))]
     if not os.path.exists(EMU_LIB) or any(os.path.getmtime(d) > os.path.getmtime(EMU_LIB) for d in deps):
-        os.makedirs(os.path.dirname(EMU_LIB), exist_ok=True)
-        subprocess.run(["g++", "-std=c++20", "-O2", "-pthread", "-shared", "-fPIC", "-ffp-contract=off",
-                        "-I" + os.path.join(ROOT, "include"), "-I" + csrc, src, "-o", EMU_LIB], check=True)
+        # the harness compiles as six translation units in parallel: the entry
+        # points and five groups of row lengths (see emu.cpp)
+        bdir = os.path.dirname(EMU_LIB)
+        os.makedirs(bdir, exist_ok=True)
+        flags = ["g++", "-std=c++20", "-O2", "-pthread", "-fPIC", "-ffp-contract=off",
+                 "-I" + os.path.join(ROOT, "include"), "-I" + csrc, "-c", src]
+        objs, procs = [], []
+        for g in [None, 0, 1, 2, 3, 4]:
+            obj = os.path.join(bdir, f"emu_{'main' if g is None else g}.o")
+            objs.append(obj)
+            procs.append(subprocess.Popen(flags + ([] if g is None else [f"-DEMU_GROUP={g}"]) + ["-o", obj]))
+        assert all(p.wait() == 0 for p in procs), "emulator build failed"
+        subprocess.run(["g++", "-shared", "-pthread", "-o", EMU_LIB] + objs, check=True)
     L = ctypes.CDLL(EMU_LIB)
     L.emu_run.argtypes = [ctypes.POINTER(am.Params), ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                           ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_int]
     L.emu_forward.argtypes = [ctypes.POINTER(am.Params), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    L.emu_inside_half.argtypes = [ctypes.POINTER(am.Params), ctypes.c_void_p]
     return L
 
 
@@ -190,3 +201,23 @@ def test_emulated_radix16_row_shape(am, orc, emu, n, kind):
     assert np.linalg.norm(w - wo) / np.linalg.norm(wo) < 2e-6
     assert np.abs(m - mo).max() <= 2e-6 * np.abs(mo).max()
     assert np.abs(e - eo).max() <= 2e-6 * np.abs(eo).max()
+
+
+@pytest.mark.parametrize("n", [(8, 8), (64, 32), (128, 256), (2048, 16), (16, 2048)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_inside_half_mask_check(am, emu, n, prec):
+    """The host check that selects pruned transforms (a per-row limit instead of
+    the mask formula at every mode) against the mask itself: zero outside the
+    ellipse -> inside; one nonzero value anywhere outside -> not inside."""
+    nx, ny = n
+    mask = np.array([[am.mask_value(nx, ny, "half", ix, iy) for ix in range(nx // 2 + 1)] for iy in range(ny)])
+    p = am.Params(nx, ny, 1.0, 1.0, 0.1, 1.0, 1.0, 1.0, 0.0, 0.0, 0, 1, prec)
+    dt = np.complex128 if prec else np.complex64
+    rng = np.random.default_rng(nx * 7 + ny)
+    w = ((rng.standard_normal(mask.shape) + 1j * rng.standard_normal(mask.shape)) * mask).astype(dt)
+    assert emu.emu_inside_half(ctypes.byref(p), w.ctypes.data) == 1
+    outside = np.argwhere(mask == 0)
+    for iy, ix in outside[rng.choice(len(outside), size=min(20, len(outside)), replace=False)]:
+        v = w.copy()
+        v[iy, ix] = 1e-30 if rng.uniform() < 0.5 else 1e-30j
+        assert emu.emu_inside_half(ctypes.byref(p), v.ctypes.data) == 0, (iy, ix)

@@ -327,18 +327,13 @@ am_status am_batch_step(am_batch *b, int nsteps, double *energy, int *nan_member
         if (energy)
             for (int m = 0; m < b->B; m++)
                 for (int i = 0; i < k; i++) energy[(size_t)(done + i) * b->B + m] = ering[(size_t)m * k + i];
-        for (int m = 0; m < b->B; m++) {
-            if (sc[m].status) {
-                b->err = "member " + std::to_string(m) + ": a bulk input copy did not complete";
-                return AM_ERR_TIMEOUT;
-            }
+        for (int m = 0; m < b->B; m++)
             if (sc[m].nan_step >= 0) {
                 if (nan_member) *nan_member = m;
                 b->err = "member " + std::to_string(m) + ": w(0,0) is NaN after step " +
                          std::to_string(done + sc[m].nan_step);
                 return AM_ERR_NAN;
             }
-        }
         done += k;
     }
     return AM_OK;

@@ -547,10 +547,6 @@ am_status am_ragged_run(am_ragged *r, double *const *energy, int *nan_run, long 
             RaggedRun &R = r->runs[i];
             if (energy && energy[i])
                 std::memcpy(energy[i] + R.done, ering.data() + (size_t)i * k, k * sizeof(double));
-            if (sc[i].status) {
-                r->err = "run " + std::to_string(i) + ": a bulk input copy did not complete";
-                return AM_ERR_TIMEOUT;
-            }
             if (sc[i].nan_step >= 0) {
                 if (nan_run) *nan_run = i;
                 r->err = "run " + std::to_string(i) + ": w(0,0) is NaN after step " +

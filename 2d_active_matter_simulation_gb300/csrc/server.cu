@@ -323,10 +323,6 @@ bool harvest(Job &j)
     if (!o.busy) return false;
     if (cudaEventQuery(o.done) != cudaSuccess) return false;
     if (j.spec.want_energy) j.energy.insert(j.energy.end(), o.energy, o.energy + o.k);
-    if (o.sc->status && j.status == AM_OK) {
-        j.status = AM_ERR_TIMEOUT;
-        j.err = "a bulk input copy did not complete";
-    }
     if (o.sc->nan_step >= 0 && j.status == AM_OK) {
         j.status = AM_ERR_NAN;
         j.err = "w(0,0) is NaN after step " + std::to_string(j.harvested + o.sc->nan_step);

@@ -37,7 +37,7 @@ struct Scalars {
     double m_old[2], m_new[2], m_appr[2];  // scaled mean velocity Nx*Ny*<u>
     int step;                              // steps completed since set_state
     int nan_step;                          // first step whose w(0,0) is NaN, or -1
-    int status;                            // device status word: 0 ok, 2 a bulk copy did not complete
+    int status;                            // reserved device status word (0 = ok)
     int pad_;
 };
 static_assert(sizeof(Scalars) == 64, "the column pass copies Scalars as four 16-byte pieces");
@@ -138,81 +138,6 @@ AF_HD void compiler_fence() { asm volatile("" ::: "memory"); }
 AF_HD float expT(float x) { return expf(x); }
 AF_HD double expT(double x) { return exp(x); }
 
-// ------------------------------------------------ bulk copies with an mbarrier
-// A bulk asynchronous copy is executed by the SM's copy engine, not by the
-// threads' load path: `bytes` (a multiple of 16; both addresses 16-byte
-// aligned) from global to shared memory, completion counted in bytes on an
-// mbarrier in shared memory.  In the CPU execution of the kernel bodies the
-// copy is a memcpy and the barrier calls do nothing (the caller's CTA barrier
-// orders the data).
-AF_HD void mbar_init(unsigned long long *bar, unsigned count)
-{
-#ifdef __CUDA_ARCH__
-    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n"
-                 "fence.mbarrier_init.release.cluster;\n" ::"r"(b), "r"(count)
-                 : "memory");
-#else
-    (void)bar;
-    (void)count;
-#endif
-}
-// Arrive once (the init count) and announce `bytes` of incoming copies.
-AF_HD void mbar_arrive_expect(unsigned long long *bar, unsigned bytes)
-{
-#ifdef __CUDA_ARCH__
-    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
-    unsigned long long state;
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;\n"
-                 : "=l"(state)
-                 : "r"(b), "r"(bytes)
-                 : "memory");
-    (void)state;
-#else
-    (void)bar;
-    (void)bytes;
-#endif
-}
-AF_HD void bulk_g2s(void *dst_smem, const void *src, unsigned bytes, unsigned long long *bar)
-{
-#ifdef __CUDA_ARCH__
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
-    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(d),
-                 "l"(src), "r"(bytes), "r"(b)
-                 : "memory");
-#else
-    (void)bar;
-    for (unsigned i = 0; i < bytes; i++)
-        static_cast<unsigned char *>(dst_smem)[i] = static_cast<const unsigned char *>(src)[i];
-#endif
-}
-// Wait for phase `parity` of the mbarrier to complete, at most `tries`
-// try_wait rounds (each may suspend the thread for a short, bounded time);
-// false if it did not complete.
-AF_HD bool mbar_wait(unsigned long long *bar, unsigned parity, long tries)
-{
-#ifdef __CUDA_ARCH__
-    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
-    for (long i = 0; i < tries; i++) {
-        unsigned done;
-        asm volatile("{\n\t.reg .pred p;\n\t"
-                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}\n"
-                     : "=r"(done)
-                     : "r"(b), "r"(parity)
-                     : "memory");
-        if (done) return true;
-    }
-    return false;
-#else
-    (void)bar;
-    (void)parity;
-    (void)tries;
-    return true;
-#endif
-}
-
 // ------------------------------------------------------------------ row pass
 // One row y per group of TPC threads; a complex FFT of length M = Nx/2 per
 // real transform (the half-length real-FFT construction).  The Hermitian pairs
@@ -253,21 +178,7 @@ struct RowPass {
         (sizeof(T) == 8 && THREADS <= 128) ? (size_t)113 * 1024 : (size_t)227 * 1024;
     static constexpr int SINGLE = (size_t)ROWS * 6 * BUFS * sizeof(cpx<T>) > SMEM_CAP ? 1 : 0;
     static constexpr int NBUF = SINGLE ? 3 : 6;
-    // Inputs by bulk copy (FP32, one row per CTA: Nx = 2048, 4096): the copy
-    // engine lands the row's three tiled input rows, contiguous in kx, in the
-    // second set of exchange buffers (untouched until the transforms' second
-    // exchange), so the threads read X(k) and X(M-k) from shared memory
-    // instead of issuing global loads that each touch 8 sectors in 8 lines.
-    // A raw row holds kx = 0..M and the rest of its last tile (RAWS slots); the
-    // three run RAWS_OVER slots past the buffers, then the mbarrier.
-    static constexpr bool BULK = sizeof(T) == 4 && ROWS == 1 && !SINGLE;
-    static constexpr int RAWS = M + Tile<T>::W;
-    static constexpr int RAWS_OVER = 3 * RAWS > 3 * BUFS ? 3 * RAWS - 3 * BUFS : 0;
-    static constexpr size_t BAR_OFF = (size_t)(NBUF * BUFS + RAWS_OVER) * sizeof(cpx<T>);
-    static constexpr size_t smem_bytes()
-    {
-        return BULK ? BAR_OFF + 16 : (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>);
-    }
+    static constexpr size_t smem_bytes() { return (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>); }
 
     // C2R pre-processing of X(k), X(M-k): Z(k) = E + i O with
     // E = X(k) + conj X(M-k), O = (X(k) - conj X(M-k)) exp(2 pi i k / Nx).
@@ -445,46 +356,11 @@ struct RowPass {
         const cpx<T> wj = ldtw(a.twx, j);
         cpx<T> v[3][R];
         const cpx<T> *src[3] = {a.fy, a.fx, a.fa};
-        if constexpr (BULK) {
-            cpx<T> *raw = rbase + 3 * BUFS;   // = b1[0].d; field f at raw + f * RAWS
-            auto *bar = reinterpret_cast<unsigned long long *>(smem + BAR_OFF);
-            constexpr int W = Tile<T>::W;
-            const int ntile = a.kxp / W + 1;   // tiles that carry data
-            if (tid == 0) {
-                mbar_init(bar, 1);
-                mbar_arrive_expect(bar, (unsigned)(3 * ntile * W * sizeof(cpx<T>)));
-            }
-            sync();
-            if (tid < 32) {
-                for (int i = tid; i < 3 * ntile; i += 32) {
-                    const int f = i / ntile, t = i - f * ntile;
-                    bulk_g2s(raw + f * RAWS + t * W, src[f] + ((size_t)t * ny + y) * W, W * sizeof(cpx<T>), bar);
-                }
-            }
-#ifdef __CUDA_ARCH__
-            if (!mbar_wait(bar, 0, 1L << 22) && j == 0) a.sc->status = 2;
-#else
-            sync();
-#endif
 #pragma unroll
-            for (int f = 0; f < 3; f++) {
-                cpx<T> A[R], B[R];
-                const cpx<T> *rf = raw + f * RAWS;
-#pragma unroll
-                for (int r = 0; r < R; r++) {
-                    const int k = j + r * TPC;
-                    A[r] = k <= a.kxp ? rf[k] : mk<T>(0, 0);
-                    B[r] = M - k <= a.kxp ? rf[M - k] : mk<T>(0, 0);
-                }
-                pack_pairs(v[f], A, B, wj, j);
-            }
-        } else {
-#pragma unroll
-            for (int f = 0; f < 3; f++) {
-                cpx<T> A[R], B[R];
-                load_pairs(A, B, src[f], j, y, ny, a.kxp);
-                pack_pairs(v[f], A, B, wj, j);
-            }
+        for (int f = 0; f < 3; f++) {
+            cpx<T> A[R], B[R];
+            load_pairs(A, B, src[f], j, y, ny, a.kxp);
+            pack_pairs(v[f], A, B, wj, j);
         }
         FFTi::template run_multi<3, SINGLE>(v, j, 0, b0, b1, a.twx, 2, sync);
 

@@ -76,6 +76,25 @@ AF_HD cpx<T> cmul(cpx<T> a, cpx<T> b) { return mk(a.x * b.x - a.y * b.y, a.x * b
 // a * conj(b)
 template <typename T>
 AF_HD cpx<T> cmulc(cpx<T> a, cpx<T> b) { return mk(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+// FP32 complex products on the packed FP32x2 pipe: a product of both halves,
+// then a fused multiply-add of both halves -- two roundings per component, as
+// the scalar product-then-fma.
+template <>
+AF_HD cpx<float> cmul(cpx<float> a, cpx<float> b)
+{
+    const float2 t = __fmul2_rn(make_float2(a.x, a.x), make_float2(b.x, b.y));
+    const float2 r = __ffma2_rn(make_float2(a.y, a.y), make_float2(-b.y, b.x), t);
+    return mk(r.x, r.y);
+}
+template <>
+AF_HD cpx<float> cmulc(cpx<float> a, cpx<float> b)
+{
+    const float2 t = __fmul2_rn(make_float2(a.x, a.y), make_float2(b.x, b.x));
+    const float2 r = __ffma2_rn(make_float2(a.y, a.x), make_float2(b.y, -b.y), t);
+    return mk(r.x, r.y);
+}
+#endif
 template <typename T>
 AF_HD cpx<T> conj(cpx<T> a) { return mk(a.x, -a.y); }
 template <typename T>

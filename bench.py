@@ -282,12 +282,39 @@ def run_ours(args):
                                       PARAMS["alpha"], PARAMS["beta"], gamma0=PARAMS["gamma0"],
                                       gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"], precision=PRECISION),
                        nsteps=10)
-    sim = am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"], PARAMS["beta"],
-                    gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"], precision=PRECISION)
-    sim.set_stream(stream.cuda_stream)
     cdt = np.complex64 if PRECISION == "fp32" else np.complex128
     w0 = am.ic_bandlimited(NX, NY, SEED).astype(cdt)
-    sim.set_state(w0, (0.0, 0.0))
+
+    def new_sim():
+        sm = am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"],
+                       PARAMS["beta"], gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"],
+                       precision=PRECISION)
+        sm.set_stream(stream.cuda_stream)
+        sm.set_state(w0, (0.0, 0.0))
+        return sm
+
+    # The autotuner times back-to-back steps with the fields resident in L2
+    # (the production case).  The timed region below flushes the L2 before
+    # every step, so the column shapes are re-timed under that condition
+    # (untimed, 10 flushed steps each) and the fastest there is used.
+    flushed = {}
+    for shape in tune[0]:
+        am.set_column_shape(PRECISION, NY, shape)
+        trial = new_sim()
+        trial.step_async(3)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+        with torch.cuda.stream(stream):
+            for a_, b_ in evs:
+                flush.zero_()
+                a_.record(stream)
+                trial.step_async(1)
+                b_.record(stream)
+        stream.synchronize()
+        flushed[shape] = sum(a_.elapsed_time(b_) for a_, b_ in evs) / len(evs)
+        trial.close()
+    col_shape = min(flushed, key=flushed.get)
+    am.set_column_shape(PRECISION, NY, col_shape)
+    sim = new_sim()
 
     # warm-up
     sim.step_async(max(args.warmup, 0))
@@ -410,8 +437,8 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if PRECISION == "fp32" else "f64", "data": "synthetic",
         "config": workload_config(),
         "timing": "CUDA events on the solver stream, one CUDA graph (8 kernels) per step",
-        "tuning": {"column_shape": tune[1], "autotune_ms_per_step": tune[0], "row_shape": tune[3],
-                   "autotune_row_ms_per_step": tune[2]},
+        "tuning": {"column_shape": col_shape, "autotune_column_shape": tune[1], "autotune_ms_per_step": tune[0],
+                   "flushed_ms_per_step": flushed, "row_shape": tune[3], "autotune_row_ms_per_step": tune[2]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_source": traffic_src, "kernel": dom,
                      "algorithmic_bytes_per_launch": dom_bytes,

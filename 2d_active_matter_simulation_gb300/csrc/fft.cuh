@@ -99,6 +99,14 @@ template <typename T>
 AF_HD cpx<T> conj(cpx<T> a) { return mk(a.x, -a.y); }
 template <typename T>
 AF_HD cpx<T> scale(cpx<T> a, T s) { return mk(a.x * s, a.y * s); }
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+template <>
+AF_HD cpx<float> scale(cpx<float> a, float s)
+{
+    const float2 r = __fmul2_rn(make_float2(a.x, a.y), make_float2(s, s));
+    return mk(r.x, r.y);
+}
+#endif
 
 // Multiply by exp(SIGN * 2 pi i Q / R) for compile-time Q, R (R <= 32).
 // Multiples of pi/2 are exact sign swaps; the remaining angles are multiples
@@ -133,6 +141,13 @@ AF_HD cpx<T> rot(cpx<T> a)
         constexpr double cs = quad == 0 ? c0 : quad == 1 ? -s0 : quad == 2 ? -c0 : s0;
         constexpr double sn = quad == 0 ? s0 : quad == 1 ? c0 : quad == 2 ? -s0 : -c0;
         const T c = (T)cs, s = (T)(SIGN * sn);
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+        if constexpr (sizeof(T) == 4) {   // packed FP32x2: product, then fma (as cmul)
+            const float2 t = __fmul2_rn(make_float2(a.x, a.x), make_float2(c, s));
+            const float2 r = __ffma2_rn(make_float2(a.y, a.y), make_float2(-s, c), t);
+            return mk(r.x, r.y);
+        }
+#endif
         return mk(a.x * c - a.y * s, a.x * s + a.y * c);
     }
 }

@@ -368,16 +368,43 @@ struct RowPass {
         // 2n + 1 (imaginary part), n = j + r * TPC.  P replaces uy, Q replaces ux.
         T se = 0, sx = 0, sy = 0;
         const T lam = a.lam_s, bet = a.beta_s;
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+        if constexpr (sizeof(T) == 4) {
+            // the two points of a complex value as the halves of packed FP32x2
+            // operations; the row sums accumulate per half and meet at the end
+            float2 se2 = make_float2(0.f, 0.f), sx2 = se2, sy2 = se2;
+            const float2 lam2 = make_float2(lam, lam), bet2 = make_float2(bet, bet);
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            T ux0 = v[1][r].x, uy0 = v[0][r].x, w0 = v[2][r].x;
-            T ux1 = v[1][r].y, uy1 = v[0][r].y, w1 = v[2][r].y;
-            T s0 = ux0 * ux0 + uy0 * uy0, s1 = ux1 * ux1 + uy1 * uy1;
-            se += s0 + s1;
-            sx += s0 * ux0 + s1 * ux1;
-            sy += s0 * uy0 + s1 * uy1;
-            v[0][r] = mk(lam * w0 * ux0 + bet * s0 * uy0, lam * w1 * ux1 + bet * s1 * uy1);
-            v[1][r] = mk(lam * w0 * uy0 - bet * s0 * ux0, lam * w1 * uy1 - bet * s1 * ux1);
+            for (int r = 0; r < R; r++) {
+                const float2 ux = make_float2(v[1][r].x, v[1][r].y), uy = make_float2(v[0][r].x, v[0][r].y);
+                const float2 w = make_float2(v[2][r].x, v[2][r].y);
+                const float2 q = __ffma2_rn(uy, uy, __fmul2_rn(ux, ux));   // |u|^2
+                se2 = __fadd2_rn(se2, q);
+                sx2 = __ffma2_rn(q, ux, sx2);
+                sy2 = __ffma2_rn(q, uy, sy2);
+                const float2 lw = __fmul2_rn(lam2, w), bq = __fmul2_rn(bet2, q);
+                const float2 P2 = __ffma2_rn(bq, uy, __fmul2_rn(lw, ux));
+                const float2 Q2 = __ffma2_rn(make_float2(-bq.x, -bq.y), ux, __fmul2_rn(lw, uy));
+                v[0][r] = mk(P2.x, P2.y);
+                v[1][r] = mk(Q2.x, Q2.y);
+            }
+            se = se2.x + se2.y;
+            sx = sx2.x + sx2.y;
+            sy = sy2.x + sy2.y;
+        } else
+#endif
+        {
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                T ux0 = v[1][r].x, uy0 = v[0][r].x, w0 = v[2][r].x;
+                T ux1 = v[1][r].y, uy1 = v[0][r].y, w1 = v[2][r].y;
+                T s0 = ux0 * ux0 + uy0 * uy0, s1 = ux1 * ux1 + uy1 * uy1;
+                se += s0 + s1;
+                sx += s0 * ux0 + s1 * ux1;
+                sy += s0 * uy0 + s1 * uy1;
+                v[0][r] = mk(lam * w0 * ux0 + bet * s0 * uy0, lam * w1 * ux1 + bet * s1 * uy1);
+                v[1][r] = mk(lam * w0 * uy0 - bet * s0 * ux0, lam * w1 * uy1 - bet * s1 * ux1);
+            }
         }
 
         // ---- row sums of |u|^2, |u|^2 ux, |u|^2 uy over the row

@@ -24,7 +24,17 @@ CLI_PATH = os.path.join(HERE, "lib", "actflow")
 (AM_OK, AM_ERR_ARG, AM_ERR_CUDA, AM_ERR_NAN, AM_ERR_IO, AM_ERR_SPEC, AM_ERR_OOM, AM_ERR_UNSUPPORTED,
  AM_ERR_TIMEOUT) = range(9)
 ORDER = {"arrival": 0, "shortest": 1}
-FP32, FP64 = 0, 1
+FP32, FP64, DF64 = 0, 1, 2   # am_precision; DF64: double-float (two floats per real)
+PRECISIONS = {"fp32": FP32, "fp64": FP64, "df64": DF64}
+
+
+def _prec(precision):
+    """am_precision of a name ("fp32", "fp64", "df64") or of the enum value."""
+    if precision in PRECISIONS:
+        return PRECISIONS[precision]
+    if precision in (FP32, FP64, DF64):
+        return int(precision)
+    raise ValueError(f"unknown precision {precision!r}")
 DEALIAS = {"reference": 0, "half": 1, "none": 2}
 # integrating factors: per value in the state precision (lin_func) or precomputed in double
 IF_FACTORS = {"auto": 0, "float": 1, "double": 2}
@@ -195,7 +205,7 @@ class Solver:
     def __init__(self, nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None,
                  dealias="reference", precision="fp32", if_factors="auto"):
         form = FORM_REFERENCE if gamma0 is None else FORM_GENERAL
-        self.precision = FP64 if precision in ("fp64", FP64) else FP32
+        self.precision = _prec(precision)
         self.params = Params(nx, ny, lx, ly, dt, lam, alpha, beta,
                              0.0 if gamma0 is None else gamma0, 0.0 if gamma2 is None else gamma2,
                              form, DEALIAS[dealias] if isinstance(dealias, str) else int(dealias),
@@ -204,8 +214,8 @@ class Solver:
         self.nx, self.ny = nx, ny
         self.h = ctypes.c_void_p()
         _check(lib.am_create(ctypes.byref(self.params), ctypes.byref(self.h)), None, "am_create")
-        self.cdtype = np.complex128 if self.precision == FP64 else np.complex64
-        self.rdtype = np.float64 if self.precision == FP64 else np.float32
+        self.cdtype = np.complex64 if self.precision == FP32 else np.complex128
+        self.rdtype = np.float32 if self.precision == FP32 else np.float64
 
     def close(self):
         if self.h:
@@ -403,7 +413,7 @@ class Server:
         j.nsteps = int(nsteps)
         keep = None
         if w_hat is not None:
-            keep = np.ascontiguousarray(w_hat, dtype=np.complex128 if params.precision == FP64 else np.complex64)
+            keep = np.ascontiguousarray(w_hat, dtype=np.complex64 if params.precision == FP32 else np.complex128)
             j.w_hat = keep.ctypes.data
         j.mean[0], j.mean[1] = mean
         j.seed, j.kmin, j.kmax, j.rms = int(seed), kmin, kmax, rms
@@ -416,7 +426,7 @@ class Server:
     def wait(self, jid, timeout=-1.0):
         """Result dict of request jid: status, times, mean, state (if kept), energy (if kept)."""
         nx, ny, prec, nsteps, ws, we = self._jobs[jid]
-        w = np.zeros((ny, nx // 2 + 1), dtype=np.complex128 if prec == FP64 else np.complex64) if ws else None
+        w = np.zeros((ny, nx // 2 + 1), dtype=np.complex64 if prec == FP32 else np.complex128) if ws else None
         e = np.zeros(max(nsteps, 1)) if we else None
         r = JobResult()
         st = lib.am_server_wait(self.h, jid, timeout, ctypes.byref(r), w.ctypes.data if ws else None,
@@ -454,13 +464,13 @@ COLUMN_SHAPES = ("wide", "narrow", "wide8")   # "wide8": wide tiles, radix-8 pas
 
 def set_column_shape(precision, ny, shape):
     """Column-pass launch shape for new simulations of this precision and Ny."""
-    prec = FP64 if precision in ("fp64", FP64) else FP32
+    prec = _prec(precision)
     _check(lib.am_set_column_shape(prec, ny, COLUMN_SHAPES.index(shape) if isinstance(shape, str) else int(shape)),
            None, "am_set_column_shape")
 
 
 def column_shape(precision, ny):
-    prec = FP64 if precision in ("fp64", FP64) else FP32
+    prec = _prec(precision)
     v = lib.am_column_shape(prec, ny)
     return COLUMN_SHAPES[v] if v >= 0 else None
 
@@ -470,13 +480,13 @@ ROW_SHAPES = ("radix8", "radix16")   # "radix16": FP32, Nx >= 1024
 
 def set_row_shape(precision, nx, shape):
     """Row-pass launch shape for new simulations of this precision and Nx."""
-    prec = FP64 if precision in ("fp64", FP64) else FP32
+    prec = _prec(precision)
     _check(lib.am_set_row_shape(prec, nx, ROW_SHAPES.index(shape) if isinstance(shape, str) else int(shape)),
            None, "am_set_row_shape")
 
 
 def row_shape(precision, nx):
-    prec = FP64 if precision in ("fp64", FP64) else FP32
+    prec = _prec(precision)
     v = lib.am_row_shape(prec, nx)
     return ROW_SHAPES[v] if v >= 0 else None
 
@@ -499,7 +509,7 @@ def make_params(nx, ny, lx, ly, dt, lam, alpha, beta, gamma0=None, gamma2=None, 
     return Params(nx, ny, lx, ly, dt, lam, alpha, beta, 0.0 if gamma0 is None else gamma0,
                   0.0 if gamma2 is None else gamma2, form,
                   DEALIAS[dealias] if isinstance(dealias, str) else int(dealias),
-                  FP64 if precision in ("fp64", FP64) else FP32,
+                  _prec(precision),
                   IF_FACTORS[if_factors] if isinstance(if_factors, str) else int(if_factors))
 
 
@@ -524,8 +534,8 @@ def read_spec(directory):
 
 
 def write_snapshot(path, w_hat, mean, precision="fp32"):
-    prec = FP64 if precision in ("fp64", FP64) else FP32
-    w = np.ascontiguousarray(w_hat, dtype=np.complex128 if prec == FP64 else np.complex64)
+    prec = _prec(precision)
+    w = np.ascontiguousarray(w_hat, dtype=np.complex64 if prec == FP32 else np.complex128)
     ny, nxh = w.shape
     m = np.array(mean, dtype=np.float64)
     _check(lib.am_write_snapshot(path.encode(), 2 * (nxh - 1), ny, prec, w.ctypes.data, _dptr(m)), None,
@@ -533,15 +543,15 @@ def write_snapshot(path, w_hat, mean, precision="fp32"):
 
 
 def read_snapshot(path, nx, ny, precision="fp32"):
-    prec = FP64 if precision in ("fp64", FP64) else FP32
-    w = np.zeros((ny, nx // 2 + 1), dtype=np.complex128 if prec == FP64 else np.complex64)
+    prec = _prec(precision)
+    w = np.zeros((ny, nx // 2 + 1), dtype=np.complex64 if prec == FP32 else np.complex128)
     m = np.zeros(2, dtype=np.float64)
     _check(lib.am_read_snapshot(path.encode(), nx, ny, prec, w.ctypes.data, _dptr(m)), None, "am_read_snapshot")
     return w, m
 
 
 def append_energy(path, m0, dt, energy, precision="fp32"):
-    prec = FP64 if precision in ("fp64", FP64) else FP32
+    prec = _prec(precision)
     e = np.ascontiguousarray(energy, dtype=np.float64)
     _check(lib.am_append_energy(path.encode(), m0, len(e), dt, _dptr(e), prec), None, "am_append_energy")
 

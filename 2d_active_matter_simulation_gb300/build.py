@@ -20,15 +20,19 @@ LIB = os.path.join(HERE, "lib")
 OBJ = os.path.join(LIB, "obj")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC] + ARCH
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-diag-suppress", "20013",
+              "-I" + INCLUDE, "-I" + CSRC] + ARCH
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + CSRC]
 
 # the kernel tables are split by transform length so that the heavy units
 # compile in parallel (the 2048- and 4096-point ones take the longest)
-CUDA_UNITS = ["kernels_f32_12.cu", "kernels_f32_11.cu", "kernels_f64_12.cu", "kernels_f64_11.cu",
+CUDA_UNITS = ["kernels_df_12.cu", "kernels_df_11.cu", "kernels_df_10.cu", "kernels_df_9.cu",
+              "kernels_f32_12.cu", "kernels_f32_11.cu", "kernels_f64_12.cu", "kernels_f64_11.cu",
+              "kernels_df_8.cu", "kernels_df_7.cu", "kernels_df_6.cu", "kernels_df_3_5.cu",
               "kernels_f32_10.cu", "kernels_batch_9_10.cu", "kernels_f32_3_6.cu", "kernels_f32_7_8.cu",
               "kernels_f32_9.cu", "kernels_f64_3_8.cu", "kernels_f64_9_10.cu",
-              "kernels_batch.cu", "kernels_queue.cu", "kernels_f32.cu", "kernels_f64.cu", "actflow_api.cu",
+              "kernels_batch.cu", "kernels_queue.cu", "kernels_f32.cu", "kernels_f64.cu", "kernels_df.cu",
+              "actflow_api.cu",
               "noalloc.cu", "batch.cu",
               "ragged.cu", "server.cu"]
 HOST_UNITS = ["spec.cpp", "io.cpp", "driver.cpp", "cli.cpp"]

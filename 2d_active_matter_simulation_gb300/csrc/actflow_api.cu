@@ -19,6 +19,7 @@
 #include <new>
 #include <random>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "actflow.h"
@@ -47,7 +48,7 @@ struct am_handle {
     int nxh = 0, nt = 0, W = 0, lognx = 0, logny = 0;
     int colv = 0;                  // column-pass launch shape (0 wide, 1 narrow, 2 wide radix 8)
     int rowv = 0;                  // row-pass launch shape (0 radix 8, 1 radix 16 with stashes)
-    bool fp64 = false;
+    int prec = AM_FP32;            // am_precision
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int device = 0;
@@ -65,7 +66,23 @@ struct am_handle {
     // kernel arguments (scalar part filled at create)
     StepArgs<float> a32{};
     StepArgs<double> a64{};
+    StepArgs<df> adf{};
 };
+
+// Calls f with a value of the state type of precision prec: float (AM_FP32),
+// double (AM_FP64) or double-float (AM_DF64).
+template <class F>
+static am_status with_type(int prec, F &&f)
+{
+    if (prec == AM_FP64) return f(double{});
+    if (prec == AM_DF64) return f(df{});
+    return f(float{});
+}
+
+// Host-side element type of a state of type T: double-float states are
+// exchanged with the host as double.
+template <typename T>
+using HostT = std::conditional_t<std::is_same_v<T, df>, double, T>;
 
 static am_status cuda_fail(am_handle *h, cudaError_t e, const char *what)
 {
@@ -87,6 +104,8 @@ template <>
 StepArgs<float> &args_of<float>(am_handle *h) { return h->a32; }
 template <>
 StepArgs<double> &args_of<double>(am_handle *h) { return h->a64; }
+template <>
+StepArgs<df> &args_of<df>(am_handle *h) { return h->adf; }
 
 template <typename T>
 static const KernelTable<T> &table();
@@ -94,6 +113,8 @@ template <>
 const KernelTable<float> &table<float>() { return kernels_f32(); }
 template <>
 const KernelTable<double> &table<double>() { return kernels_f64(); }
+template <>
+const KernelTable<df> &table<df>() { return kernels_df(); }
 
 template <typename T>
 static am_status alloc_and_tables(am_handle *h)
@@ -283,9 +304,10 @@ static void choose_pruning(am_handle *h, bool on)
 template <typename T>
 static am_status set_state_impl(am_handle *h, const void *w_hat, const double mean[2])
 {
-    choose_pruning<T>(h, state_inside_half_mask<T>((const T *)w_hat, h->p.nx, h->p.ny));
+    choose_pruning<T>(h, state_inside_half_mask<HostT<T>>((const HostT<T> *)w_hat, h->p.nx, h->p.ny));
     const size_t bytes = (size_t)h->p.ny * h->nxh * sizeof(cpx<T>);
     CK(h, cudaMemcpyAsync(h->stage, w_hat, bytes, cudaMemcpyHostToDevice, h->stream));
+    if constexpr (std::is_same_v<T, df>) df_from_double_async(h->stage, (size_t)2 * h->p.ny * h->nxh, h->stream);
     table<T>().tile<<<1024, 256, 0, h->stream>>>((const cpx<T> *)h->stage, (cpx<T> *)h->u0, h->p.ny, h->nxh,
                                                  h->nt);
     CK(h, cudaGetLastError());
@@ -305,6 +327,7 @@ static am_status set_state_real_impl(am_handle *h, const void *w_real, const dou
     const KernelTable<T> &K = table<T>();
     const size_t bytes = (size_t)h->p.ny * h->p.nx * sizeof(T);
     CK(h, cudaMemcpyAsync(h->stage, w_real, bytes, cudaMemcpyHostToDevice, h->stream));
+    if constexpr (std::is_same_v<T, df>) df_from_double_async(h->stage, (size_t)h->p.ny * h->p.nx, h->stream);
     const LaunchShape &rs = K.rowfwd_shape[h->lognx];
     K.rowfwd[h->lognx]<<<(h->p.ny + rs.per_block - 1) / rs.per_block, rs.threads, rs.smem, h->stream>>>(
         (const T *)h->stage, (cpx<T> *)h->P, (const cpx<T> *)h->twx, h->p.ny, h->nt);
@@ -329,6 +352,10 @@ static am_status get_state_impl(am_handle *h, void *w_hat, double mean[2])
     table<T>().untile<<<1024, 256, 0, h->stream>>>((const cpx<T> *)h->u0, (cpx<T> *)h->stage, h->p.ny, h->nxh,
                                                    h->nt);
     CK(h, cudaGetLastError());
+    if constexpr (std::is_same_v<T, df>) {
+        df_to_double_async(h->stage, (size_t)2 * h->p.ny * h->nxh, h->stream);
+        CK(h, cudaGetLastError());
+    }
     const size_t bytes = (size_t)h->p.ny * h->nxh * sizeof(cpx<T>);
     if (w_hat) CK(h, cudaMemcpyAsync(w_hat, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream));
     Scalars s;
@@ -376,30 +403,38 @@ static am_status step_impl(am_handle *h, int nsteps, double *energy, int *nan_st
 namespace af {
 
 namespace {
-// [fp64][log2 Ny]: 0 wide, 1 narrow, 2 wide radix 8; seeded with the measured rule
-std::atomic<int> g_colv[2][LOG_MAX + 1] = {
+// [precision][log2 Ny]: 0 wide, 1 narrow, 2 wide radix 8; seeded with the measured rule
+std::atomic<int> g_colv[3][LOG_MAX + 1] = {
+    {{1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {0}, {0}},
     {{1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {0}, {0}},
     {{1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {1}, {0}, {0}}};
 static_assert(LOG_MAX == 12, "seed table covers log2 Ny = 0..12");
+int pidx(int prec) { return prec == AM_FP64 ? 1 : prec == AM_DF64 ? 2 : 0; }
 }  // namespace
 
-int col_variant(bool fp64, int logny) { return g_colv[fp64 ? 1 : 0][logny].load(std::memory_order_relaxed); }
-void set_col_variant(bool fp64, int logny, int v) { g_colv[fp64 ? 1 : 0][logny].store(v); }
+int col_variant(int prec, int logny) { return g_colv[pidx(prec)][logny].load(std::memory_order_relaxed); }
+void set_col_variant(int prec, int logny, int v) { g_colv[pidx(prec)][logny].store(v); }
 
-// True if column-pass shape v is built for this precision (wide radix 8: FP32 only).
-bool col_variant_built(bool fp64, int v) { return v >= 0 && v < NCOLV && !(fp64 && v == 2); }
+// True if column-pass shape v is built for this precision and log2 Ny: wide
+// radix 8 is FP32 only; double-float has the seeded shape of each length only.
+bool col_variant_built(int prec, int logny, int v)
+{
+    if (v < 0 || v >= NCOLV) return false;
+    if (prec == AM_DF64) return v == (logny < 11 ? 1 : 0);
+    return !(prec == AM_FP64 && v == 2);
+}
 
 namespace {
-// [fp64][log2 Nx]: 0 radix 8, 1 radix 16 with stashes; seeded with radix 8
-std::atomic<int> g_rowv[2][LOG_MAX + 1] = {};
+// [precision][log2 Nx]: 0 radix 8, 1 radix 16 with stashes; seeded with radix 8
+std::atomic<int> g_rowv[3][LOG_MAX + 1] = {};
 }  // namespace
 
-int row_variant(bool fp64, int lognx) { return g_rowv[fp64 ? 1 : 0][lognx].load(std::memory_order_relaxed); }
-void set_row_variant(bool fp64, int lognx, int v) { g_rowv[fp64 ? 1 : 0][lognx].store(v); }
+int row_variant(int prec, int lognx) { return g_rowv[pidx(prec)][lognx].load(std::memory_order_relaxed); }
+void set_row_variant(int prec, int lognx, int v) { g_rowv[pidx(prec)][lognx].store(v); }
 // Radix 16 with stashes: FP32, Nx >= 1024.
-bool row_variant_built(bool fp64, int lognx, int v)
+bool row_variant_built(int prec, int lognx, int v)
 {
-    return v == 0 || (v == 1 && !fp64 && lognx >= ROWS_LOG_MIN && lognx <= LOG_MAX);
+    return v == 0 || (v == 1 && prec == AM_FP32 && lognx >= ROWS_LOG_MIN && lognx <= LOG_MAX);
 }
 
 }  // namespace af
@@ -452,7 +487,7 @@ cudaStream_t handle_stream(const am_handle *h) { return h ? h->stream : nullptr;
 am_status handle_enqueue_chunk(am_handle *h, int k, double *energy_host, void *scalars_host, cudaEvent_t done)
 {
     if (!h || k < 1 || k > ECAP || !scalars_host || !h->state_loaded) return AM_ERR_ARG;
-    am_status st = h->fp64 ? build_graph<double>(h) : build_graph<float>(h);
+    am_status st = with_type(h->prec, [&](auto t) { return build_graph<decltype(t)>(h); });
     if (st) return st;
     CK(h, cudaMemsetAsync(&h->sc->step, 0, sizeof(int), h->stream));
     for (int i = 0; i < k; i++) CK(h, cudaGraphLaunch(h->graph, h->stream));
@@ -499,7 +534,7 @@ am_status am_create(const am_params *p, am_handle **out)
     if (!is_pow2(p->nx) || !is_pow2(p->ny) || p->nx < (1 << LOG_MIN) || p->ny < (1 << LOG_MIN) ||
         p->nx > (1 << LOG_MAX) || p->ny > (1 << LOG_MAX))
         return AM_ERR_UNSUPPORTED;
-    if (p->precision != AM_FP32 && p->precision != AM_FP64) return AM_ERR_ARG;
+    if (p->precision != AM_FP32 && p->precision != AM_FP64 && p->precision != AM_DF64) return AM_ERR_ARG;
     if (p->dealias < 0 || p->dealias > 2 || (p->form != AM_FORM_REFERENCE && p->form != AM_FORM_GENERAL))
         return AM_ERR_ARG;
     if (!(p->lx > 0) || !(p->ly > 0) || !std::isfinite(p->dt)) return AM_ERR_ARG;
@@ -509,18 +544,18 @@ am_status am_create(const am_params *p, am_handle **out)
     am_handle *h = new (std::nothrow) am_handle();
     if (!h) return AM_ERR_OOM;
     h->p = *p;
-    h->fp64 = p->precision == AM_FP64;
+    h->prec = p->precision;
     h->lognx = ilog2(p->nx);
     h->logny = ilog2(p->ny);
-    h->colv = col_variant(h->fp64, h->logny);
-    h->rowv = row_variant(h->fp64, h->lognx);
+    h->colv = col_variant(h->prec, h->logny);
+    h->rowv = row_variant(h->prec, h->lognx);
     cudaGetDevice(&h->device);
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete h;
         return AM_ERR_CUDA;
     }
     h->own_stream = true;
-    am_status st = h->fp64 ? alloc_and_tables<double>(h) : alloc_and_tables<float>(h);
+    am_status st = with_type(h->prec, [&](auto t) { return alloc_and_tables<decltype(t)>(h); });
     if (st) {
         am_destroy(h);
         return st;
@@ -572,14 +607,14 @@ am_status am_set_stream(am_handle *h, void *stream)
 am_status am_set_state(am_handle *h, const void *w_hat, const double mean[2])
 {
     if (!h || !w_hat) return AM_ERR_ARG;
-    return h->fp64 ? set_state_impl<double>(h, w_hat, mean) : set_state_impl<float>(h, w_hat, mean);
+    return with_type(h->prec, [&](auto t) { return set_state_impl<decltype(t)>(h, w_hat, mean); });
 }
 
 am_status am_set_state_real(am_handle *h, const void *w_real, const double mean[2], int mask_and_zero_mean)
 {
     if (!h || !w_real) return AM_ERR_ARG;
-    return h->fp64 ? set_state_real_impl<double>(h, w_real, mean, mask_and_zero_mean)
-                   : set_state_real_impl<float>(h, w_real, mean, mask_and_zero_mean);
+    return with_type(h->prec,
+                     [&](auto t) { return set_state_real_impl<decltype(t)>(h, w_real, mean, mask_and_zero_mean); });
 }
 
 am_status am_get_state(am_handle *h, void *w_hat, double mean[2])
@@ -589,7 +624,7 @@ am_status am_get_state(am_handle *h, void *w_hat, double mean[2])
         h->err = "no state loaded";
         return AM_ERR_ARG;
     }
-    return h->fp64 ? get_state_impl<double>(h, w_hat, mean) : get_state_impl<float>(h, w_hat, mean);
+    return with_type(h->prec, [&](auto t) { return get_state_impl<decltype(t)>(h, w_hat, mean); });
 }
 
 am_status am_step(am_handle *h, int nsteps, double *energy, int *nan_step)
@@ -599,16 +634,14 @@ am_status am_step(am_handle *h, int nsteps, double *energy, int *nan_step)
         h->err = "no state loaded";
         return AM_ERR_ARG;
     }
-    return h->fp64 ? step_impl<double>(h, nsteps, energy, nan_step, true)
-                   : step_impl<float>(h, nsteps, energy, nan_step, true);
+    return with_type(h->prec, [&](auto t) { return step_impl<decltype(t)>(h, nsteps, energy, nan_step, true); });
 }
 
 am_status am_step_async(am_handle *h, int nsteps)
 {
     if (!h || nsteps < 0) return AM_ERR_ARG;
     if (!h->state_loaded) return AM_ERR_ARG;
-    return h->fp64 ? step_impl<double>(h, nsteps, nullptr, nullptr, false)
-                   : step_impl<float>(h, nsteps, nullptr, nullptr, false);
+    return with_type(h->prec, [&](auto t) { return step_impl<decltype(t)>(h, nsteps, nullptr, nullptr, false); });
 }
 
 am_status am_sync(am_handle *h)
@@ -638,9 +671,10 @@ am_status am_step_profiled(am_handle *h, int nsteps, double row_ms[4], double co
     if (!st) {
         ce = cudaEventRecordWithFlags(ev[0], h->stream, cudaEventRecordExternal);
         for (int s = 1; s <= 4 && !st && ce == cudaSuccess; s++) {
-            st = h->fp64 ? launch_row<double>(h) : launch_row<float>(h);
+            st = with_type(h->prec, [&](auto t) { return launch_row<decltype(t)>(h); });
             if (!st) ce = cudaEventRecordWithFlags(ev[2 * s - 1], h->stream, cudaEventRecordExternal);
-            if (!st && ce == cudaSuccess) st = h->fp64 ? launch_col<double>(h, s) : launch_col<float>(h, s);
+            if (!st && ce == cudaSuccess)
+                st = with_type(h->prec, [&](auto t) { return launch_col<decltype(t)>(h, s); });
             if (!st && ce == cudaSuccess) ce = cudaEventRecordWithFlags(ev[2 * s], h->stream, cudaEventRecordExternal);
         }
         cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
@@ -678,7 +712,7 @@ am_status am_row_passes_async(am_handle *h, int reps)
 {
     if (!h || reps < 0) return AM_ERR_ARG;
     if (!h->state_loaded) return AM_ERR_ARG;
-    am_status st = h->fp64 ? build_rows_graph<double>(h) : build_rows_graph<float>(h);
+    am_status st = with_type(h->prec, [&](auto t) { return build_rows_graph<decltype(t)>(h); });
     if (st) return st;
     for (int i = 0; i < reps; i++) CK(h, cudaGraphLaunch(h->graph_rows, h->stream));
     return AM_OK;
@@ -687,37 +721,37 @@ am_status am_row_passes_async(am_handle *h, int reps)
 am_status am_set_column_shape(int precision, int ny, int shape)
 {
     if (!is_pow2(ny) || ny < (1 << LOG_MIN) || ny > (1 << LOG_MAX) || shape < 0 || shape >= NCOLV ||
-        (precision != AM_FP32 && precision != AM_FP64))
+        (precision != AM_FP32 && precision != AM_FP64 && precision != AM_DF64))
         return AM_ERR_ARG;
-    if (!col_variant_built(precision == AM_FP64, shape)) return AM_ERR_UNSUPPORTED;
-    set_col_variant(precision == AM_FP64, ilog2(ny), shape);
+    if (!col_variant_built(precision, ilog2(ny), shape)) return AM_ERR_UNSUPPORTED;
+    set_col_variant(precision, ilog2(ny), shape);
     return AM_OK;
 }
 
 int am_column_shape(int precision, int ny)
 {
     if (!is_pow2(ny) || ny < (1 << LOG_MIN) || ny > (1 << LOG_MAX) ||
-        (precision != AM_FP32 && precision != AM_FP64))
+        (precision != AM_FP32 && precision != AM_FP64 && precision != AM_DF64))
         return -1;
-    return col_variant(precision == AM_FP64, ilog2(ny));
+    return col_variant(precision, ilog2(ny));
 }
 
 am_status am_set_row_shape(int precision, int nx, int shape)
 {
     if (!is_pow2(nx) || nx < (1 << LOG_MIN) || nx > (1 << LOG_MAX) || shape < 0 || shape >= NROWV ||
-        (precision != AM_FP32 && precision != AM_FP64))
+        (precision != AM_FP32 && precision != AM_FP64 && precision != AM_DF64))
         return AM_ERR_ARG;
-    if (!row_variant_built(precision == AM_FP64, ilog2(nx), shape)) return AM_ERR_UNSUPPORTED;
-    set_row_variant(precision == AM_FP64, ilog2(nx), shape);
+    if (!row_variant_built(precision, ilog2(nx), shape)) return AM_ERR_UNSUPPORTED;
+    set_row_variant(precision, ilog2(nx), shape);
     return AM_OK;
 }
 
 int am_row_shape(int precision, int nx)
 {
     if (!is_pow2(nx) || nx < (1 << LOG_MIN) || nx > (1 << LOG_MAX) ||
-        (precision != AM_FP32 && precision != AM_FP64))
+        (precision != AM_FP32 && precision != AM_FP64 && precision != AM_DF64))
         return -1;
-    return row_variant(precision == AM_FP64, ilog2(nx));
+    return row_variant(precision, ilog2(nx));
 }
 
 // Time nsteps graph replays of the handle's step (after two warm-up steps).
@@ -759,11 +793,11 @@ am_status am_autotune(const am_params *p, int nsteps, double ms_col[3], double m
     double best = 0;
     bool first = true;
     for (int v = 0; v < NCOLV && !st; v++) {
-        if (!col_variant_built(h->fp64, v)) {
+        if (!col_variant_built(h->prec, h->logny, v)) {
             if (ms_col) ms_col[v] = -1;   // not built for this precision
             continue;
         }
-        st = h->fp64 ? use_col_variant<double>(h, v) : use_col_variant<float>(h, v);
+        st = with_type(h->prec, [&](auto t) { return use_col_variant<decltype(t)>(h, v); });
         double per = 0;
         if (!st) st = time_steps(h, nsteps, e0, e1, &per);
         if (st) break;
@@ -774,14 +808,14 @@ am_status am_autotune(const am_params *p, int nsteps, double ms_col[3], double m
             first = false;
         }
     }
-    if (!st) st = h->fp64 ? use_col_variant<double>(h, bestc) : use_col_variant<float>(h, bestc);
+    if (!st) st = with_type(h->prec, [&](auto t) { return use_col_variant<decltype(t)>(h, bestc); });
     first = true;
     for (int v = 0; v < NROWV && !st; v++) {
-        if (!row_variant_built(h->fp64, h->lognx, v)) {
+        if (!row_variant_built(h->prec, h->lognx, v)) {
             if (ms_row) ms_row[v] = -1;
             continue;
         }
-        st = h->fp64 ? use_row_variant<double>(h, v) : use_row_variant<float>(h, v);
+        st = with_type(h->prec, [&](auto t) { return use_row_variant<decltype(t)>(h, v); });
         double per = 0;
         if (!st) st = time_steps(h, nsteps, e0, e1, &per);
         if (st) break;
@@ -796,8 +830,8 @@ am_status am_autotune(const am_params *p, int nsteps, double ms_col[3], double m
     if (e1) cudaEventDestroy(e1);
     am_destroy(h);
     if (!st) {
-        set_col_variant(p->precision == AM_FP64, ilog2(p->ny), bestc);
-        set_row_variant(p->precision == AM_FP64, ilog2(p->nx), bestr);
+        set_col_variant(p->precision, ilog2(p->ny), bestc);
+        set_row_variant(p->precision, ilog2(p->nx), bestr);
     }
     return st;
 }
@@ -809,7 +843,7 @@ long long am_device_bytes(const am_handle *h) { return h ? h->bytes : 0; }
 long long am_footprint_bytes(const am_params *p)
 {
     if (!p || !is_pow2(p->nx) || !is_pow2(p->ny)) return -1;
-    const bool f64 = p->precision == AM_FP64;
+    const bool f64 = p->precision != AM_FP32;   // FP64 and double-float: 8-byte reals
     const size_t cs = f64 ? sizeof(cpx<double>) : sizeof(cpx<float>), rs = f64 ? sizeof(double) : sizeof(float);
     const int W = f64 ? Tile<double>::W : Tile<float>::W;
     const int nxh = p->nx / 2 + 1, nt = (nxh + W - 1) / W;
@@ -822,7 +856,7 @@ long long am_footprint_bytes(const am_params *p)
 int am_kx_carried(const am_handle *h)
 {
     if (!h) return -1;
-    return h->fp64 ? h->a64.kxp : h->a32.kxp;
+    return h->prec == AM_FP64 ? h->a64.kxp : h->prec == AM_DF64 ? h->adf.kxp : h->a32.kxp;
 }
 
 am_status am_ic_bandlimited(int nx, int ny, unsigned long long seed, double kmin, double kmax, double rms,

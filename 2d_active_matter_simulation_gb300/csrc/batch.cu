@@ -157,8 +157,8 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
     b->ny = p0.ny;
     b->lognx = lx;
     b->logny = ly;
-    b->colv = col_variant(false, ly);
-    b->rowv = row_variant(false, lx);
+    b->colv = col_variant(AM_FP32, ly);
+    b->rowv = row_variant(AM_FP32, lx);
     b->loaded.assign(nmembers, 0);
     b->inside.assign(nmembers, 0);
     auto fail = [&](am_status s) {

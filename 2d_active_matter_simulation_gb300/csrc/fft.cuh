@@ -5,7 +5,8 @@
 // with real threads and barriers.  Only the qualifier macros differ.
 //
 // Conventions
-//  * cpx<T>: complex number {x = real, y = imaginary}, T = float or double.
+//  * cpx<T>: complex number {x = real, y = imaginary}, T = float, double or
+//    df (double-float, dfloat.cuh).
 //  * A length-L transform is computed by TPC = L/R threads; thread j holds the
 //    elements j + r*TPC (r = 0..R-1) in registers on entry and on exit
 //    ("cyclic distribution").  The first pass may use a smaller radix R1 (each
@@ -20,6 +21,8 @@
 #pragma once
 
 #include <type_traits>
+
+#include "dfloat.cuh"
 
 #ifdef __CUDACC__
 #define AF_HD __host__ __device__ __forceinline__
@@ -270,6 +273,15 @@ AF_HD cpx<double> ldtw(const cpx<double> *tw, int idx)
     return tw[idx];
 #endif
 }
+AF_HD cpx<df> ldtw(const cpx<df> *tw, int idx)
+{
+#ifdef __CUDA_ARCH__
+    float4 v = __ldg(reinterpret_cast<const float4 *>(tw) + idx);
+    return mk(df(v.x, v.y), df(v.z, v.w));
+#else
+    return tw[idx];
+#endif
+}
 
 // Length-L (L = 2^LOGL) block FFT on data distributed cyclically over TPC =
 // L/R threads.  `sync` is the block barrier (called identically by every
@@ -277,7 +289,8 @@ AF_HD cpx<double> ldtw(const cpx<double> *tw, int idx)
 // m < L * TWS; the transform uses every TWS-th entry.
 // Twiddle powers w[r] = W^{r k} (r = 1..R-1) for one pass, from the table
 // entry at r * step.  FP32: the powers 1, 2, 4, 8 are loaded and the others
-// formed by at most three complex products (error a few ulp); FP64: all loaded.
+// formed by at most three complex products (error a few ulp); FP64 and
+// double-float (8-byte reals): all loaded.
 template <int R, typename T>
 AF_HD void twiddles(cpx<T> *w, const cpx<T> *tw, int step)
 {

@@ -47,7 +47,7 @@ const char *HELP =
     "  initial_condition (random [n] | blank | continue [T_ext [snapshot]] |\n"
     "                     bandlimited <seed> [kmin kmax rms]),\n"
     "  save_directory,\n"
-    "  optional: precision (fp32|fp64), dealias (reference|half|none), Gamma0, Gamma2,\n"
+    "  optional: precision (fp32|fp64|df64), dealias (reference|half|none), Gamma0, Gamma2,\n"
     "            snapshot_binary (1: exact ActTurb_snap{i}.raw beside each snapshot)\n"
     "--------------------------------------------------\n";
 
@@ -197,13 +197,13 @@ int cli_main(int argc, char **argv)
         std::cerr << "Error: dt_snap must be at least dt/2 (snapshot interval of 0 steps)." << std::endl;
         return 1;
     }
-    const bool fp64 = s.precision == AM_FP64;
+    const bool fp64 = s.precision != AM_FP32;   // host values in double (FP64, double-float)
     std::cout << "--------------------------------------------------\n"
               << "T = " << fmt_g(s.T) << "\ndt = " << fmt_g(s.dt) << "\nM = " << M << "\nLx = " << fmt_g(s.Lx)
               << "\nLy = " << fmt_g(s.Ly) << "\nNx = " << s.Nx << "\nNy = " << s.Ny
               << "\nalpha = " << fmt_g(s.alpha) << "\nbeta = " << fmt_g(s.beta) << "\nlambda = " << fmt_g(s.lambda)
               << "\ninitial condition: " << s.initial << "\ntotal amount of snapshots: " << M / snap
-              << "\nprecision: " << (fp64 ? "fp64" : "fp32")
+              << "\nprecision: " << (s.precision == AM_DF64 ? "df64" : fp64 ? "fp64" : "fp32")
               << "\n--------------------------------------------------" << std::endl;
 
     am_params p{};

@@ -166,19 +166,19 @@ am_status am_spec_read(const char *dir, am_spec *out, char *err, int errlen)
 am_status am_write_snapshot(const char *path, int nx, int ny, int precision, const void *w_hat, const double mean[2])
 {
     if (!path || !w_hat || !mean) return AM_ERR_ARG;
-    return afh::write_snapshot(path, nx, ny, precision == AM_FP64, w_hat, mean) ? AM_OK : AM_ERR_IO;
+    return afh::write_snapshot(path, nx, ny, precision != AM_FP32, w_hat, mean) ? AM_OK : AM_ERR_IO;
 }
 
 am_status am_read_snapshot(const char *path, int nx, int ny, int precision, void *w_hat, double mean[2])
 {
     if (!path || !w_hat || !mean) return AM_ERR_ARG;
-    return afh::read_snapshot(path, nx, ny, precision == AM_FP64, w_hat, mean) ? AM_OK : AM_ERR_IO;
+    return afh::read_snapshot(path, nx, ny, precision != AM_FP32, w_hat, mean) ? AM_OK : AM_ERR_IO;
 }
 
 am_status am_append_energy(const char *path, long long m0, int count, float dt, const double *energy, int precision)
 {
     if (!path || (count > 0 && !energy)) return AM_ERR_ARG;
-    return afh::append_energy(path, m0, count, dt, energy, precision == AM_FP64) ? AM_OK : AM_ERR_IO;
+    return afh::append_energy(path, m0, count, dt, energy, precision != AM_FP32) ? AM_OK : AM_ERR_IO;
 }
 
 }  // extern "C"

@@ -4,7 +4,7 @@
 // reference keys and their parsing (stof into float, stoi into int) are kept;
 // an unknown key -- including a blank line -- is an error, as in the reference.
 // Extension keys accepted in addition (the reference rejects them):
-//   precision:  fp32 | fp64
+//   precision:  fp32 | fp64 | df64 (double-float)
 //   dealias:    reference | half | none
 //   Gamma0:, Gamma2:  select the general linear operator -alpha - G0 k^2 - G2 k^4
 //   snapshot_binary:  1 = also write ActTurb_snap{i}.raw (exact, used by continue)
@@ -79,6 +79,7 @@ int read_spec(const std::string &dir, Spec &s, std::string &err)
             next();
             if (val == "fp32") s.precision = AM_FP32;
             else if (val == "fp64") s.precision = AM_FP64;
+            else if (val == "df64") s.precision = AM_DF64;
             else ok = false;
         } else if (line == "dealias:") {
             next();

@@ -4,6 +4,7 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 #include <vector>
 
 #include "actflow.h"
@@ -78,10 +79,17 @@ void host_setup(const am_params &p, HostTables<T> &t, StepArgs<T> &a, int ecap)
     a.ecap = ecap;
     // FFT normalisation folded into lambda and beta in T, as the reference does
     // (ActFlow_V3-2.cu:434-436): lambda / N^2, beta / N^3.
-    const T fnorm = (T)(nx * ny);
-    a.lam_s = (T)p.lambda / (fnorm * fnorm);
-    a.beta_s = (T)p.beta / (fnorm * fnorm * fnorm);
     const double nd = (double)nx * (double)ny;
+    if constexpr (std::is_same_v<T, df>) {
+        // double-float: formed in double and split (host code does no
+        // double-float arithmetic)
+        a.lam_s = T(p.lambda / (nd * nd));
+        a.beta_s = T(p.beta / (nd * nd * nd));
+    } else {
+        const T fnorm = (T)(nx * ny);
+        a.lam_s = (T)p.lambda / (fnorm * fnorm);
+        a.beta_s = (T)p.beta / (fnorm * fnorm * fnorm);
+    }
     a.beta_sd = p.beta / (nd * nd * nd);
     a.dt = (T)p.dt;
     a.alpha = (T)p.alpha;

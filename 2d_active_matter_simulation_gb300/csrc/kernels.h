@@ -1,6 +1,7 @@
-// Dispatch tables of the compiled step and set-up kernels, one per precision.
-// The tables are filled in kernels_f32.cu / kernels_f64.cu, which instantiate
-// the kernel templates for every supported power-of-two length.
+// Dispatch tables of the compiled step and set-up kernels, one per precision
+// (FP32, FP64, double-float).  The tables are filled in kernels_f32.cu /
+// kernels_f64.cu / kernels_df.cu, which instantiate the kernel templates for
+// every supported power-of-two length.
 #pragma once
 #include <cstddef>
 
@@ -65,6 +66,13 @@ struct KernelTable {
 
 const KernelTable<float> &kernels_f32();
 const KernelTable<double> &kernels_f64();
+const KernelTable<df> &kernels_df();
+
+// In-place conversion of n reals between double and double-float (both 8
+// bytes, so an array keeps its size and layout) on a CUDA stream; the state of
+// an AM_DF64 simulation is exchanged with the host as double.
+void df_from_double_async(void *data, size_t n, void *stream);
+void df_to_double_async(void *data, size_t n, void *stream);
 
 // Fillers of the tables, one per translation unit (ranges of log2 lengths).
 void fill_f32_3_6(KernelTable<float> &t);
@@ -77,6 +85,14 @@ void fill_f64_3_8(KernelTable<double> &t);
 void fill_f64_9_10(KernelTable<double> &t);
 void fill_f64_11(KernelTable<double> &t);
 void fill_f64_12(KernelTable<double> &t);
+void fill_df_3_5(KernelTable<df> &t);
+void fill_df_6(KernelTable<df> &t);
+void fill_df_7(KernelTable<df> &t);
+void fill_df_8(KernelTable<df> &t);
+void fill_df_9(KernelTable<df> &t);
+void fill_df_10(KernelTable<df> &t);
+void fill_df_11(KernelTable<df> &t);
+void fill_df_12(KernelTable<df> &t);
 
 // Batched forms of the step kernels: one launch covers every member of an
 // ensemble (blockIdx.y = member), each member's arguments read from a device
@@ -90,17 +106,17 @@ struct BatchTable {
 };
 
 // Column-pass launch shape (0 wide, 1 narrow, 2 wide radix 8) used for new
-// simulations of this precision and log2 Ny: a process-wide table seeded with
-// the measured rule (narrow below Ny = 2048) and updated by am_autotune /
-// am_set_column_shape.
-int col_variant(bool fp64, int logny);
-void set_col_variant(bool fp64, int logny, int v);
-bool col_variant_built(bool fp64, int v);
+// simulations of this precision (am_precision) and log2 Ny: a process-wide
+// table seeded with the measured rule (narrow below Ny = 2048) and updated by
+// am_autotune / am_set_column_shape.
+int col_variant(int prec, int logny);
+void set_col_variant(int prec, int logny, int v);
+bool col_variant_built(int prec, int logny, int v);
 // Row-pass launch shape for new simulations of this precision and log2 Nx
 // (0 radix 8, 1 radix 16 with stashes), as col_variant.
-int row_variant(bool fp64, int lognx);
-void set_row_variant(bool fp64, int lognx, int v);
-bool row_variant_built(bool fp64, int lognx, int v);
+int row_variant(int prec, int lognx);
+void set_row_variant(int prec, int lognx, int v);
+bool row_variant_built(int prec, int lognx, int v);
 
 const BatchTable &kernels_batch_f32();
 

@@ -1,7 +1,8 @@
 // Kernel entry points and dispatch-table construction.  The table of a
 // precision is filled by several translation units, each instantiating a range
-// of transform lengths (kernels_f32_*.cu, kernels_f64_*.cu), so that they
-// compile in parallel; kernels_f32.cu / kernels_f64.cu assemble the tables.
+// of transform lengths (kernels_f32_*.cu, kernels_f64_*.cu, kernels_df_*.cu),
+// so that they compile in parallel; kernels_f32.cu / kernels_f64.cu /
+// kernels_df.cu assemble the tables.
 #pragma once
 #include "kernels.h"
 #include "setup_kernels.cuh"
@@ -112,8 +113,14 @@ struct Fill {
             t.row[LOG][1] = k_rows<T, LOG>;
             t.row_shape[LOG][1] = {RowPassS<T, LOG>::THREADS, RowPassS<T, LOG>::smem_bytes(), RowPassS<T, LOG>::ROWS};
         }
-        fill_col<0>(t);
-        fill_col<1>(t);
+        if constexpr (std::is_same_v<T, df>) {
+            // double-float: the default shape of the length only (each
+            // instantiation of these long unrolled kernels costs compile time)
+            fill_col<(LOG < 11 ? 1 : 0)>(t);
+        } else {
+            fill_col<0>(t);
+            fill_col<1>(t);
+        }
         if constexpr (sizeof(T) == 4) fill_col<2>(t);   // wide radix 8: FP32 only
         t.rowfwd[LOG] = k_rowfwd<T, LOG>;
         t.rowfwd_shape[LOG] = {RowFwd<T, LOG>::THREADS, RowFwd<T, LOG>::smem_bytes(), RowFwd<T, LOG>::ROWS};

@@ -180,9 +180,10 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
     a.inv_2n3 = 1.0 / (2.0 * nd * nd * nd);
 
     const KernelTable<T> &K = table<T>();
-    const int rowv = row_variant(sizeof(T) == 8, lx2);
+    constexpr int prec = sizeof(T) == 8 ? AM_FP64 : AM_FP32;
+    const int rowv = row_variant(prec, lx2);
     const LaunchShape &rs = K.row_shape[lx2][rowv];
-    const int colv = col_variant(sizeof(T) == 8, ly2);
+    const int colv = col_variant(prec, ly2);
     const LaunchShape &cs = K.col_shape[ly2][colv];
     if (rs.smem > 48 * 1024 &&
         cudaFuncSetAttribute((const void *)K.row[lx2][rowv], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs.smem))
@@ -224,6 +225,7 @@ extern "C" am_status am_step_noalloc(const am_params *p, void *w_hat, double *me
     if (!pow2(p->nx) || !pow2(p->ny) || p->nx < (1 << LOG_MIN) || p->ny < (1 << LOG_MIN) ||
         p->nx > (1 << LOG_MAX) || p->ny > (1 << LOG_MAX))
         return AM_ERR_UNSUPPORTED;
+    if (p->precision == AM_DF64) return AM_ERR_UNSUPPORTED;   // double-float: handles only
     if (p->precision != AM_FP32 && p->precision != AM_FP64) return AM_ERR_ARG;
     if (p->dealias < 0 || p->dealias > 2 || (p->form != AM_FORM_REFERENCE && p->form != AM_FORM_GENERAL))
         return AM_ERR_ARG;

@@ -324,8 +324,8 @@ am_status am_ragged_create(const am_params *params, const long long *nsteps, int
         key[keys[c]] = (int)c;
         r->cls[c].lognx = keys[c].first;
         r->cls[c].logny = keys[c].second;
-        r->cls[c].colv = col_variant(false, keys[c].second);
-        r->cls[c].rowv = row_variant(false, keys[c].first);
+        r->cls[c].colv = col_variant(AM_FP32, keys[c].second);
+        r->cls[c].rowv = row_variant(AM_FP32, keys[c].first);
     }
     size_t total = 0, stage = 0;
     for (int i = 0; i < nruns; i++) {

@@ -8,10 +8,11 @@
 //
 //  * admission (thread "admit"): pending requests are admitted in arrival
 //    order (or shortest job first) while their device footprint fits the HBM
-//    budget and an active slot is free.  FP64 requests (about 20 times the GPU
-//    time of an FP32 request of the same size) have a lane of their own: at
-//    most max_active_fp64 of them are active at once, and an FP64 request
-//    waiting for that lane does not hold back the FP32 requests behind it.  Admission creates the request's
+//    budget and an active slot is free.  FP64 and double-float requests
+//    (about 20 and 5 times the GPU time of an FP32 request of the same size)
+//    share a lane of their own: at most max_active_fp64 of them are active at
+//    once, and a request waiting for that lane does not hold back the FP32
+//    requests behind it.  Admission creates the request's
 //    handle, builds its initial field (the seeded band-limited generator or
 //    the caller's state) and loads it.  Finished handles are destroyed on this
 //    thread too (stream-ordered frees: no wait for other requests' work).
@@ -83,7 +84,7 @@ struct Job {
 
 size_t state_bytes(const am_params &p)
 {
-    return (size_t)p.ny * (p.nx / 2 + 1) * (p.precision == AM_FP64 ? 16 : 8);
+    return (size_t)p.ny * (p.nx / 2 + 1) * (p.precision != AM_FP32 ? 16 : 8);
 }
 
 }  // namespace
@@ -100,7 +101,7 @@ struct am_server {
     long long next_id = 1;
     long long used = 0;                            // reserved device bytes
     int active = 0;                                // admitted and not yet reaped
-    int active_fp64 = 0;                           // of which FP64
+    int active_fp64 = 0;                           // of which FP64 or double-float
     bool stop = false;
     long long gps_done = 0, jobs_done = 0, peak_used = 0;
     int peak_active = 0;
@@ -124,20 +125,26 @@ void free_chunk(Chunk &c)
 
 // Steps per chunk: about 20 ms of estimated GPU time (at most the configured
 // chunk), so that a chunk of a large request never holds the host for long.
-// Estimated step time per grid point on this GPU: 7e-8 ms FP32, 1.5e-6 ms FP64.
+// Estimated step time per grid point on this GPU: 7e-8 ms FP32, 1.5e-6 ms FP64,
+// 3.5e-7 ms double-float.
 int chunk_steps_for(const am_server *s, const am_params &p)
 {
-    const double ms = (double)p.nx * p.ny * (p.precision == AM_FP64 ? 1.5e-6 : 7e-8);
+    const double per = p.precision == AM_FP64 ? 1.5e-6 : p.precision == AM_DF64 ? 3.5e-7 : 7e-8;
+    const double ms = (double)p.nx * p.ny * per;
     const double k = 20.0 / (ms > 0 ? ms : 1.0);
     return k >= s->cfg.chunk_steps ? s->cfg.chunk_steps : k < 1.0 ? 1 : (int)k;
 }
 
 // Work of a request in FP32 grid-point-steps (an FP64 step costs about 20
-// FP32 steps of the same grid on this GPU).
+// FP32 steps of the same grid on this GPU, a double-float step about 5).
 double work_of(const am_job &j)
 {
-    return (double)j.params.nx * j.params.ny * (double)j.nsteps * (j.params.precision == AM_FP64 ? 20.0 : 1.0);
+    const double f = j.params.precision == AM_FP64 ? 20.0 : j.params.precision == AM_DF64 ? 5.0 : 1.0;
+    return (double)j.params.nx * j.params.ny * (double)j.nsteps * f;
 }
+
+// Requests that take the FP64 lane: the 8-byte precisions.
+bool in_fp64_lane(const am_params &p) { return p.precision != AM_FP32; }
 
 // Stream priority of a request: one level per factor 10 of work above 1e8
 // grid-point-steps, the least work on the greatest priority.  The block
@@ -182,7 +189,7 @@ am_status prepare(am_server *s, Job &j)
         std::vector<double> w((size_t)p.ny * (p.nx / 2 + 1) * 2);
         st = am_ic_bandlimited(p.nx, p.ny, j.spec.seed, j.spec.kmin, j.spec.kmax, j.spec.rms, w.data());
         if (!st) {
-            if (p.precision == AM_FP64) {
+            if (p.precision != AM_FP32) {   // FP64, double-float: double on the host
                 st = am_set_state(j.h, w.data(), j.spec.mean);
             } else {
                 std::vector<float> f(w.size());
@@ -244,18 +251,18 @@ void admit_loop(am_server *s)
             }
             s->used -= j->footprint;
             s->active--;
-            if (j->spec.params.precision == AM_FP64) s->active_fp64--;
+            if (in_fp64_lane(j->spec.params)) s->active_fp64--;
         }
         if (s->stop && s->pending.empty() && s->active == 0) return;
         // pick the next request that may be admitted
-        // (FP64 requests whose lane is full are passed over; the first request
+        // (FP64-lane requests are passed over while the lane is full; the first request
         // that may take a slot is then admitted only if its footprint fits,
         // so a large request is not overtaken indefinitely by smaller ones)
         auto pick = s->pending.end();
         if (!s->pending.empty() && s->active < s->cfg.max_active) {
             const bool lane64 = s->active_fp64 < s->cfg.max_active_fp64;
             auto eligible = [&](const std::shared_ptr<Job> &j) {
-                return lane64 || j->spec.params.precision != AM_FP64;
+                return lane64 || !in_fp64_lane(j->spec.params);
             };
             if (s->cfg.order == AM_ORDER_SHORTEST_FIRST) {
                 for (auto it = s->pending.begin(); it != s->pending.end(); ++it)
@@ -275,7 +282,7 @@ void admit_loop(am_server *s)
         s->pending.erase(pick);
         s->used += j->footprint;
         s->active++;
-        if (j->spec.params.precision == AM_FP64) s->active_fp64++;
+        if (in_fp64_lane(j->spec.params)) s->active_fp64++;
         s->peak_used = std::max(s->peak_used, s->used);
         s->peak_active = std::max(s->peak_active, s->active);
         lk.unlock();
@@ -426,7 +433,8 @@ am_status am_server_submit(am_server *s, const am_job *job, long long *id)
     const am_params &p = job->params;
     const long long fp = am_footprint_bytes(&p);
     if (fp < 0 || p.nx < 8 || p.ny < 8 || p.nx > 4096 || p.ny > 4096) return AM_ERR_UNSUPPORTED;
-    if (job->nsteps < 0 || (p.precision != AM_FP32 && p.precision != AM_FP64)) return AM_ERR_ARG;
+    if (job->nsteps < 0 || (p.precision != AM_FP32 && p.precision != AM_FP64 && p.precision != AM_DF64))
+        return AM_ERR_ARG;
     auto j = std::make_shared<Job>();
     j->spec = *job;
     j->footprint = fp;

@@ -137,6 +137,19 @@ AF_HD void compiler_fence() { asm volatile("" ::: "memory"); }
 
 AF_HD float expT(float x) { return expf(x); }
 AF_HD double expT(double x) { return exp(x); }
+// double-float: the exponential in double, split once (only the per-value
+// integrating factors use it; the default for this precision is the table)
+AF_HD df expT(df x) { return df(exp((double)x)); }
+
+#ifdef __CUDA_ARCH__
+// Butterfly shuffle of a value of the state precision across a warp.
+__device__ __forceinline__ float shfl_xor(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ df shfl_xor(df v, int o)
+{
+    return df(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
+}
+#endif
 
 // ------------------------------------------------------------------ row pass
 // One row y per group of TPC threads; a complex FFT of length M = Nx/2 per
@@ -289,9 +302,9 @@ struct RowPass {
         if constexpr (TPC >= 32) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                t0 += __shfl_xor_sync(0xffffffffu, t0, o);
-                t1 += __shfl_xor_sync(0xffffffffu, t1, o);
-                t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+                t0 += shfl_xor(t0, o);
+                t1 += shfl_xor(t1, o);
+                t2 += shfl_xor(t2, o);
             }
             constexpr int NW = TPC / 32;
             sync();
@@ -608,9 +621,9 @@ struct RowPassS {
         if constexpr (TPC >= 32) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                t0 += __shfl_xor_sync(0xffffffffu, t0, o);
-                t1 += __shfl_xor_sync(0xffffffffu, t1, o);
-                t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+                t0 += shfl_xor(t0, o);
+                t1 += shfl_xor(t1, o);
+                t2 += shfl_xor(t2, o);
             }
             if ((j & 31) == 0) {
                 scratch[(j >> 5) * 3 + 0] = t0;
@@ -687,6 +700,16 @@ struct RowAcc<float> {
         const float h = __shfl_xor_sync(0xffffffffu, hi, o), l = __shfl_xor_sync(0xffffffffu, lo, o);
         add2(h, l);
     }
+#endif
+};
+template <>
+struct RowAcc<df> {   // double-float path: the sums in double-float
+    df v{};
+    AF_HD void add(df x) { v += x; }
+    AF_HD void add(const RowAcc &o) { v += o.v; }
+    AF_HD double value() const { return (double)v; }
+#ifdef __CUDA_ARCH__
+    __device__ void add_xor(int o) { v += shfl_xor(v, o); }
 #endif
 };
 

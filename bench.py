@@ -112,6 +112,10 @@ PRESETS = {
 }
 
 
+# arithmetic type of each precision path (df64: double-float, two FP32 per real)
+DTYPES = {"fp32": "f32", "fp64": "f64", "df64": "f32x2 (double-float)"}
+
+
 def apply_preset(cfg, precision, n=None):
     global NX, NY, SEED, PRECISION, WORKLOAD
     p = PRESETS[cfg]
@@ -401,6 +405,13 @@ def run_ours(args):
     launches = sim.launches_per_step * args.steps
     sim.close()
 
+    # ---- the FP64-class paths on the same workload (headline only): FP64 and
+    # double-float, timed like the steps above (L2 flushed, CUDA events), and
+    # how far apart their states are after those steps
+    paths = None
+    if not args.no_compare and nrep == 1 and PRECISION == "fp32" and NX == 2048 and NY == 2048:
+        paths = precision_paths(am, stream, flush, max(args.steps, 10))
+
     # ---- CPU baseline: the oracle on the host cores, bounded sample
     cpu = None
     if not args.no_cpu and PRECISION == "fp32" and nrep == 1:
@@ -434,7 +445,7 @@ def run_ours(args):
     out = {
         "metric": "grid-point-steps/s", "value": value, "unit": "grid-point-steps/s", "n_gpus": nrep,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if PRECISION == "fp32" else "f64", "data": "synthetic",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPES[PRECISION], "data": "synthetic",
         "config": workload_config(),
         "timing": "CUDA events on the solver stream, one CUDA graph (8 kernels) per step",
         "tuning": {"column_shape": col_shape, "autotune_column_shape": tune[1], "autotune_ms_per_step": tune[0],
@@ -457,15 +468,52 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if paths is not None:
+        out["precision_paths"] = paths
     out.update(compare)
     if world()[1] == 0:
         print(json.dumps(out), flush=True)
 
 
+def precision_paths(am, stream, flush, nsteps):
+    """ms per step of the FP64 and double-float paths on the headline workload
+    (seeded field, default launch shapes, L2 flushed before every step) and
+    the relative L2 distance of the two states after nsteps + 3 steps."""
+    import numpy as np
+    import torch
+
+    w0 = am.ic_bandlimited(NX, NY, SEED)
+    out, states = {}, {}
+    for prec in ("fp64", "df64"):
+        sim = am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"],
+                        PARAMS["beta"], gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"],
+                        precision=prec)
+        sim.set_stream(stream.cuda_stream)
+        sim.set_state(w0, (0.0, 0.0))
+        sim.step_async(3)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+        with torch.cuda.stream(stream):
+            for a_, b_ in ev:
+                flush.zero_()
+                a_.record(stream)
+                sim.step_async(1)
+                b_.record(stream)
+        stream.synchronize()
+        ms = sum(a_.elapsed_time(b_) for a_, b_ in ev) / nsteps
+        states[prec] = sim.get_state()[0]
+        sim.close()
+        out[prec] = {"ms_per_step": ms, "value": NX * NY / (ms / 1e3), "dtype": DTYPES[prec]}
+    out["df64_speedup_over_fp64"] = out["fp64"]["ms_per_step"] / out["df64"]["ms_per_step"]
+    out["df64_vs_fp64_rel_l2"] = float(np.linalg.norm(states["df64"] - states["fp64"]) /
+                                       np.linalg.norm(states["fp64"]))
+    out["steps_compared"] = nsteps + 3
+    return out
+
+
 def run_accuracy(args):
     """Precision form: the FP32 path (bulk FFT and products in FP32, integrating
     factors computed in double and rounded, mean flow and reductions in double
-    or compensated FP32) against the FP64 path.
+    or compensated FP32) and the double-float path against the FP64 path.
 
     Short horizon: relative L2 of w_hat after 200 steps from the seeded field.
     Long horizon: the time-mean energy and the time-averaged shell spectrum
@@ -495,14 +543,15 @@ def run_accuracy(args):
     res = {"if_factors": "double, rounded (auto)"}
     # short horizon from the seeded field
     short = {}
-    for prec in ("fp32", "fp64"):
+    for prec in ("fp32", "fp64", "df64"):
         sim = solver(prec)
-        sim.set_state(w0 if prec == "fp64" else w0.astype(np.complex64))
+        sim.set_state(w0 if prec != "fp32" else w0.astype(np.complex64))
         sim.step(200)
         short[prec] = sim.get_state()[0].astype(np.complex128)
         sim.close()
     res["short_horizon_steps"] = 200
     res["w_rel_l2_200"] = float(np.linalg.norm(short["fp32"] - short["fp64"]) / np.linalg.norm(short["fp64"]))
+    res["w_rel_l2_200_df64"] = float(np.linalg.norm(short["df64"] - short["fp64"]) / np.linalg.norm(short["fp64"]))
 
     # start of the long runs
     t0 = time.perf_counter()
@@ -521,7 +570,7 @@ def run_accuracy(args):
 
     rng = np.random.default_rng(1234)
     runs = {}
-    names = ["fp32", "fp64"] + [f"twin{i}" for i in range(args.acc_twins)]
+    names = ["fp32", "fp64", "df64"] + [f"twin{i}" for i in range(args.acc_twins)]
     for name in names:
         if name.startswith("twin"):
             # one part in 1e12 per mode, Hermitian on the kx = 0 column
@@ -529,8 +578,8 @@ def run_accuracy(args):
             r[:, 0] = 0.5 * (r[:, 0] + r[(-np.arange(NY)) % NY, 0])
             start_w = s0 * (1.0 + 1e-12 * r)
         else:
-            start_w = s0 if name == "fp64" else s0.astype(np.complex64)
-        sim = solver("fp32" if name == "fp32" else "fp64")
+            start_w = s0.astype(np.complex64) if name == "fp32" else s0
+        sim = solver(name if name in ("fp32", "df64") else "fp64")
         sim.set_state(start_w, m0)
         t1 = time.perf_counter()
         e, specs, done = [], [], 0
@@ -560,6 +609,7 @@ def run_accuracy(args):
     res["window_steps"] = [args.acc_spinup + window_from, args.acc_spinup + n_total]
     res["mean_energy_fp64"] = e_ref
     res["fp32"] = diffs(runs["fp32"])
+    res["df64"] = diffs(runs["df64"])
     res["twins"] = [diffs(runs[f"twin{i}"]) for i in range(args.acc_twins)]
     if res["twins"]:
         env_e = max(t["mean_energy_rel_diff"] for t in res["twins"])
@@ -568,10 +618,14 @@ def run_accuracy(args):
         res["fp32_within_target"] = {
             "mean_energy": res["fp32"]["mean_energy_rel_diff"] <= max(0.01, env_e),
             "spectrum_l1": res["fp32"]["spectrum_l1_rel_diff"] <= max(0.01, env_s)}
+        res["df64_within_envelope"] = {
+            "mean_energy": res["df64"]["mean_energy_rel_diff"] <= env_e,
+            "spectrum_l1": res["df64"]["spectrum_l1_rel_diff"] <= env_s}
     res["energy_fp64_first_last"] = [float(ref["energy"][0]), float(ref["energy"][-1])]
     res["seconds"] = {k: v["seconds"] for k, v in runs.items()}
     res["gps_fp64"] = NX * NY * n_total / runs["fp64"]["seconds"]
     res["gps_fp32"] = NX * NY * n_total / runs["fp32"]["seconds"]
+    res["gps_df64"] = NX * NY * n_total / runs["df64"]["seconds"]
     print(json.dumps({"accuracy": res, "config": {"workload": WORKLOAD}}), flush=True)
 
 
@@ -799,7 +853,7 @@ def main():
     ap.add_argument("--acc-spinup", type=int, default=0, help="accuracy: FP64 steps before the long runs")
     ap.add_argument("--acc-twins", type=int, default=4, help="accuracy: perturbed FP64 runs (chaotic spread)")
     ap.add_argument("--config", type=int, default=1, choices=sorted(PRESETS))
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "df64"])
     ap.add_argument("--n", type=int, default=0,
                     help="configs 0/1: grid size N (N x N) instead of the preset's, e.g. 4096 (fields exceed L2)")
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="config 4: arrival window")

@@ -14,7 +14,8 @@
  *    plane, row-major [Ny][Nx/2+1] complex (re, im interleaved), rows in FFT
  *    order ky = 0, 1, ..., Ny/2, -Ny/2+1, ..., -1 (cuFFT R2C output layout,
  *    ActFlow_V3-2.cu:507, 665; snapshot layout ActFlow_V3-2.cu:1261-1262).
- *    Element type: float for AM_FP32 handles, double for AM_FP64 handles.
+ *    Element type: float for AM_FP32 handles, double for AM_FP64 and AM_DF64
+ *    handles.
  *  - mean[2]: the mean velocity scaled by Nx*Ny, i.e. the k = 0 entries of the
  *    unnormalised velocity spectra (ActFlow_V3-2.cu:1053-1054, 1263).
  *  - energy: E = sum(ux^2 + uy^2) / (2 (Nx Ny)^3) of the state at the start of
@@ -42,7 +43,14 @@ typedef enum {
     AM_ERR_TIMEOUT = 8       /* a wait ran out before the result was ready */
 } am_status;
 
-typedef enum { AM_FP32 = 0, AM_FP64 = 1 } am_precision;
+/* State precision.  AM_DF64 ("double-float") holds every real as the
+ * unevaluated sum of two floats (about 48 significant bits against double's 53)
+ * and computes with FP32 instructions only: on GB300, whose FP64 units have a
+ * small fraction of the FP32 throughput, it runs an FP64-class simulation
+ * several times faster than AM_FP64.  Its state is exchanged with the host as
+ * double; handles only (am_step_noalloc, ensembles and ragged batches refuse
+ * it); integrating factors from the double table by default. */
+typedef enum { AM_FP32 = 0, AM_FP64 = 1, AM_DF64 = 2 } am_precision;
 
 /* Dealiasing of the nonlinear term.  REFERENCE reproduces cutoff_func
  * (ActFlow_V3-2.cu:899-919) including its 32-bit overflow of the radius (every
@@ -162,7 +170,8 @@ am_status am_row_passes_async(am_handle *h, int reps);
  * cudaStream_t, NULL = default stream) and the call returns without waiting; it
  * runs the full transforms, evaluates the integrating factors per value in the
  * state's precision whatever p->if_factors asks (a table would not fit the
- * array), and reports no NaN (check mean or the energies).
+ * array), and reports no NaN (check mean or the energies).  FP32 and FP64
+ * only (AM_DF64: AM_ERR_UNSUPPORTED).
  * Calls share the array: calls that overlap on the GPU race and must be
  * serialised. */
 am_status am_step_noalloc(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy, void *stream);
@@ -236,9 +245,9 @@ typedef struct am_server_config {
     int chunk_steps;             /* largest chunk of steps (0: 256; at most 4096); each request's
                                     chunks hold about 20 ms of estimated GPU time, up to this */
     int order;                   /* am_order: admission order of pending requests */
-    int max_active_fp64;         /* FP64 requests on the GPU at once (0: max_active / 4, rounded up);
-                                    an FP64 request waiting for this lane does not hold back
-                                    the FP32 requests behind it */
+    int max_active_fp64;         /* FP64 and double-float requests on the GPU at once (0:
+                                    max_active / 4, rounded up); a request waiting for this
+                                    lane does not hold back the FP32 requests behind it */
     int reserved[4];             /* must be zero */
 } am_server_config;
 
@@ -359,7 +368,7 @@ typedef struct am_spec {
     double lambda, alpha, beta, dt_snap;
     double gamma0, gamma2;   /* extension keys Gamma0: / Gamma2: */
     int has_gamma;
-    int precision;           /* extension key precision: fp32 | fp64 */
+    int precision;           /* extension key precision: fp32 | fp64 | df64 */
     int dealias;             /* extension key dealias: reference | half | none */
     char initial[256];
     char directory[1024];
@@ -373,7 +382,8 @@ am_status am_spec_read(const char *dir, am_spec *out, char *err, int errlen);
 
 /* Write a snapshot file in the reference's text layout (save_func,
  * ActFlow_V3-2.cu:1245-1266): Ny*(Nx/2+1) pairs "re,im," then "mx,my", each in
- * the default ostream form (%g).  w_hat is float for AM_FP32, double for AM_FP64. */
+ * the default ostream form (%g).  w_hat is float for AM_FP32, double for AM_FP64
+ * and AM_DF64. */
 am_status am_write_snapshot(const char *path, int nx, int ny, int precision, const void *w_hat,
                             const double mean[2]);
 

@@ -170,9 +170,12 @@ struct Runner {
 // The harness compiles as several translation units in parallel (it is one
 // big template instantiation otherwise): with EMU_GROUP = g it instantiates
 // the row lengths of group g and exports emu_group_<g>; without it, it holds
-// the exported entry points, which call the group of the row length.
+// the exported entry points, which call the group of the row length.  Group
+// EMU_DF_GROUP holds the double-float kernels (a few grids: 32^2, 64^2, 128x32,
+// 2048x8, 8x2048), whose state is exchanged as double.
 constexpr int group_of(int lx) { return lx <= 5 ? 0 : lx <= 8 ? 1 : lx <= 10 ? 2 : lx == 11 ? 3 : 4; }
 constexpr int NGROUPS = 5;
+#define EMU_DF_GROUP 5
 
 struct Call {
     const am_params *p;
@@ -184,7 +187,30 @@ struct Call {
     int fwd, mask, colvar, rowvar;
 };
 
-#ifdef EMU_GROUP
+#if defined(EMU_GROUP) && EMU_GROUP == EMU_DF_GROUP
+template <int LX, int LY>
+int run_df(const Call &c)
+{
+    if (c.fwd) return -100;
+    const size_t n = (size_t)c.p->ny * (c.p->nx / 2 + 1) * 2;
+    double *wd = (double *)c.w;
+    std::vector<df> w(n);
+    for (size_t i = 0; i < n; i++) w[i] = df(wd[i]);
+    const int r = Runner<df, LX, LY>::run(*c.p, w.data(), c.m, c.n, c.e, c.colvar, c.rowvar);
+    for (size_t i = 0; i < n; i++) wd[i] = (double)w[i];
+    return r;
+}
+
+int dispatch_df(int lx, int ly, const Call &c)
+{
+    if (lx == 5 && ly == 5) return run_df<5, 5>(c);
+    if (lx == 6 && ly == 6) return run_df<6, 6>(c);
+    if (lx == 7 && ly == 5) return run_df<7, 5>(c);
+    if (lx == 11 && ly == 3) return run_df<11, 3>(c);
+    if (lx == 3 && ly == 11) return run_df<3, 11>(c);
+    return -100;
+}
+#elif defined(EMU_GROUP)
 template <typename T, int LX, int LY>
 int dispatch_y(const Call &c)
 {
@@ -259,7 +285,9 @@ int dispatch(int lx, int ly, const Call &c)
 #define EMU_CAT(a, b) EMU_CAT2(a, b)
 
 extern "C" {
-#ifdef EMU_GROUP
+#if defined(EMU_GROUP) && EMU_GROUP == EMU_DF_GROUP
+int emu_group_df(int lx, int ly, const Call *c) { return dispatch_df(lx, ly, *c); }
+#elif defined(EMU_GROUP)
 int EMU_CAT(emu_group_, EMU_GROUP)(int lx, int ly, const Call *c)
 {
     return c->p->precision == AM_FP64 ? dispatch<double>(lx, ly, *c) : dispatch<float>(lx, ly, *c);
@@ -270,6 +298,7 @@ int emu_group_1(int, int, const Call *);
 int emu_group_2(int, int, const Call *);
 int emu_group_3(int, int, const Call *);
 int emu_group_4(int, int, const Call *);
+int emu_group_df(int, int, const Call *);
 
 static int dispatch_all(const Call &c)
 {
@@ -278,6 +307,7 @@ static int dispatch_all(const Call &c)
     while ((1 << ly) < c.p->ny) ly++;
     int (*const groups[NGROUPS])(int, int, const Call *) = {emu_group_0, emu_group_1, emu_group_2, emu_group_3,
                                                             emu_group_4};
+    if (c.p->precision == AM_DF64) return emu_group_df(lx, ly, &c);
     return lx < 3 || lx > 12 ? -100 : groups[group_of(lx)](lx, ly, &c);
 }
 
@@ -286,7 +316,8 @@ static int dispatch_all(const Call &c)
 // 2048; otherwise the default for the length) and row-pass shape rowvar (0
 // radix 8, 1 radix 16 with stashes: FP32, Nx >= 1024).
 // Returns the first NaN step or -1; -100 for an unsupported size (8..128 each,
-// or one side 512..4096 with the other 8..16).
+// or one side 512..4096 with the other 8..16; double-float, w_hat in double:
+// 32x32, 64x64, 128x32, 2048x8, 8x2048).
 int emu_run(const am_params *p, void *w_hat, double *mean, int nsteps, double *energy, int colvar, int rowvar)
 {
     return dispatch_all(Call{p, w_hat, mean, nsteps, energy, nullptr, 0, 0, colvar, rowvar});
@@ -296,7 +327,7 @@ int emu_run(const am_params *p, void *w_hat, double *mean, int nsteps, double *e
 // state is zero at every mode the 1/2 rule removes.
 int emu_inside_half(const am_params *p, const void *w_hat)
 {
-    if (p->precision == AM_FP64) return state_inside_half_mask<double>((const double *)w_hat, p->nx, p->ny) ? 1 : 0;
+    if (p->precision != AM_FP32) return state_inside_half_mask<double>((const double *)w_hat, p->nx, p->ny) ? 1 : 0;
     return state_inside_half_mask<float>((const float *)w_hat, p->nx, p->ny) ? 1 : 0;
 }
 

@@ -107,3 +107,18 @@ def test_autotune_keeps_the_faster_shape(am):
             assert np.array_equal(wb, ws)
     finally:
         am.set_column_shape("fp32", 512, old)
+
+
+def test_double_float_has_one_column_shape_per_length(am):
+    """Double-float builds the seeded column shape of each length only
+    (narrow below Ny = 2048, wide from it); the autotuner times that one and
+    the radix-8 row shape."""
+    with pytest.raises(am.ActflowError):
+        am.set_column_shape("df64", 2048, "narrow")
+    with pytest.raises(am.ActflowError):
+        am.set_row_shape("df64", 2048, "radix16")
+    p = am.make_params(512, 2048, 2 * math.pi, 2 * math.pi, 2e-4, 3.5, -0.8, 0.01, gamma0=-0.045,
+                       gamma2=2.5e-5, dealias="half", precision="df64")
+    times, chosen, rtimes, rchosen = am.autotune(p, nsteps=3)
+    assert set(times) == {"wide"} and chosen == "wide" and times["wide"] > 0
+    assert set(rtimes) == {"radix8"} and rchosen == "radix8"

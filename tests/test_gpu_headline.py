@@ -5,11 +5,12 @@ The benchmark step: a 2048^2 grid on the [0, 2 pi)^2 box, the dimensional
 operator (Gamma0 = -0.045, Gamma2 = 2.5e-5), lambda = 3.5, alpha = -0.8,
 beta = 0.01, dt = 1e-4, the isotropic 1/2 rule with pruned transforms (the
 state is band-limited, so the passes carry kx <= Nx/4), the wide column-pass
-shape, seeded band-limited field (seed 7, rms 0.01).  Ten steps in FP32 and
-FP64 against the FP64 oracle.
+shape, seeded band-limited field (seed 7, rms 0.01).  Ten steps in FP32, FP64
+and double-float against the FP64 oracle.
 
-Tolerances: FP64 1e-10 relative (the same arithmetic, different summation
-order); FP32 2e-5 relative, the short-horizon bound the parity tests use.
+Tolerances: FP64 and double-float 1e-10 relative (the same arithmetic,
+different summation order; double-float carries about 48 bits); FP32 2e-5
+relative, the short-horizon bound the parity tests use.
 """
 import math
 
@@ -34,21 +35,21 @@ def oracle_10(orc, am):
     return w0, orc.run(p, w0, (0.0, 0.0), 10, "f64")
 
 
-@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("prec", ["fp32", "fp64", "df64"])
 def test_headline_configuration_vs_oracle(am, oracle_10, prec):
     w0, (wo, mo, eo) = oracle_10
     before = am.column_shape(prec, N)
     am.set_column_shape(prec, N, "wide")
     try:
         sim = am.Solver(N, N, L, L, DT, LAM, ALPHA, BETA, gamma0=G0, gamma2=G2, dealias="half", precision=prec)
-        sim.set_state(w0 if prec == "fp64" else w0.astype(np.complex64))
+        sim.set_state(w0 if prec != "fp32" else w0.astype(np.complex64))
         assert sim.kx_carried == N // 4   # pruned transforms, as benchmarked
         e = sim.step(10)
         w, m = sim.get_state()
         sim.close()
     finally:
         am.set_column_shape(prec, N, before)
-    tol = 1e-10 if prec == "fp64" else 2e-5
+    tol = 1e-10 if prec != "fp32" else 2e-5
     assert rel(w, wo) < tol
     assert np.abs(e - eo).max() <= tol * np.abs(eo).max()
     # the mean starts at zero and stays near it: compare it on the scale of the

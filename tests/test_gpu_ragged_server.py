@@ -120,13 +120,14 @@ def test_ragged_rejects_unsupported(am):
     p = am.make_params(2048, 2048, 1.0, 1.0, 1e-3, 1.0, -0.8, 0.01)
     with pytest.raises(am.ActflowError):
         am.Ragged([p], [3])
-    p = am.make_params(256, 256, 1.0, 1.0, 1e-3, 1.0, -0.8, 0.01, precision="fp64")
-    with pytest.raises(am.ActflowError):
-        am.Ragged([p], [3])
+    for prec in ("fp64", "df64"):
+        p = am.make_params(256, 256, 1.0, 1.0, 1e-3, 1.0, -0.8, 0.01, precision=prec)
+        with pytest.raises(am.ActflowError):
+            am.Ragged([p], [3])
 
 
 def test_footprint_matches_handle(am):
-    for nx, ny, prec in ((64, 64, "fp32"), (256, 128, "fp64"), (2048, 2048, "fp32")):
+    for nx, ny, prec in ((64, 64, "fp32"), (256, 128, "fp64"), (2048, 2048, "fp32"), (128, 512, "df64")):
         p = am.make_params(nx, ny, 1.0, 1.0, 1e-3, 1.0, -0.8, 0.01, precision=prec)
         sim = am.Solver(nx, ny, 1.0, 1.0, 1e-3, 1.0, -0.8, 0.01, precision=prec)
         assert am.footprint_bytes(p) == sim.device_bytes
@@ -137,9 +138,9 @@ def _requests(am, rng, n):
     out = []
     for i in range(n):
         nx = int(rng.choice([64, 128, 256, 512]))
-        prec = "fp64" if i % 4 == 3 else "fp32"
+        prec = "fp64" if i % 8 == 3 else "df64" if i % 8 == 7 else "fp32"
         p = _run_params(am, nx, nx, rng)
-        p.precision = am.FP64 if prec == "fp64" else am.FP32
+        p.precision = am.PRECISIONS[prec]
         out.append((p, int(rng.integers(10, 120)), 4000 + i, prec))
     return out
 

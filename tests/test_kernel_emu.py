@@ -21,14 +21,15 @@ def emu(am):
     csrc = os.path.join(ROOT, "2d_active_matter_simulation_gb300", "csrc")
     deps = [src] + [os.path.join(csrc, f) for f in os.listdir(csrc) if f.endswith((".cuh", ".h"))]
     if not os.path.exists(EMU_LIB) or any(os.path.getmtime(d) > os.path.getmtime(EMU_LIB) for d in deps):
-        # the harness compiles as six translation units in parallel: the entry
-        # points and five groups of row lengths (see emu.cpp)
+        # the harness compiles as seven translation units in parallel: the entry
+        # points, five groups of row lengths and the double-float kernels (see
+        # emu.cpp)
         bdir = os.path.dirname(EMU_LIB)
         os.makedirs(bdir, exist_ok=True)
         flags = ["g++", "-std=c++20", "-O2", "-pthread", "-fPIC", "-ffp-contract=off",
                  "-I" + os.path.join(ROOT, "include"), "-I" + csrc, "-c", src]
         objs, procs = [], []
-        for g in [None, 0, 1, 2, 3, 4]:
+        for g in [None, 0, 1, 2, 3, 4, 5]:
             obj = os.path.join(bdir, f"emu_{'main' if g is None else g}.o")
             objs.append(obj)
             procs.append(subprocess.Popen(flags + ([] if g is None else [f"-DEMU_GROUP={g}"]) + ["-o", obj]))
@@ -221,3 +222,22 @@ def test_inside_half_mask_check(am, emu, n, prec):
         v = w.copy()
         v[iy, ix] = 1e-30 if rng.uniform() < 0.5 else 1e-30j
         assert emu.emu_inside_half(ctypes.byref(p), v.ctypes.data) == 0, (iy, ix)
+
+
+@pytest.mark.parametrize("n,dealias", [((32, 32), "reference"), ((64, 64), "half"), ((128, 32), "none"),
+                                       ((2048, 8), "half"), ((8, 2048), "half")])
+def test_emulated_double_float(am, orc, emu, n, dealias):
+    """The double-float kernels (AM_DF64: two floats per real, FP32 arithmetic
+    only) against the FP64 oracle.  Double-float carries about 48 bits against
+    double's 53; the state agrees to about 5e-15 of its norm (FP32 would be off
+    by 1e-7)."""
+    nx, ny = n
+    w0 = np.fft.rfft2(np.random.default_rng(nx + 3 * ny).standard_normal((ny, nx)))
+    p = am.Params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, -0.045, 2.5e-5, 1, am.DEALIAS[dealias], am.DF64)
+    w, m, e = _emu_run(am, emu, p, w0, (3.0, 1.0), 3)
+    op = orc.make_params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, -0.045, 2.5e-5, dealias=dealias,
+                         if_double=True)
+    wo, mo, eo = orc.run(op, w0, (3.0, 1.0), 3, "f64")
+    assert np.linalg.norm(w - wo) / np.linalg.norm(wo) < 1e-13
+    assert np.abs(m - mo).max() <= 1e-13 * np.abs(mo).max()
+    assert np.abs(e - eo).max() <= 1e-13 * np.abs(eo).max()

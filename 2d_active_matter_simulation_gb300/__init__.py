@@ -475,7 +475,10 @@ def column_shape(precision, ny):
     return COLUMN_SHAPES[v] if v >= 0 else None
 
 
-ROW_SHAPES = ("radix8", "radix16")   # "radix16": FP32, Nx >= 1024
+# row-pass shapes: the three inverse transforms in lockstep (radix 8), or one
+# after another with shared-memory stashes ("sequence": FP32 radix 16,
+# double-float radix 8; Nx >= 1024)
+ROW_SHAPES = ("lockstep", "sequence")
 
 
 def set_row_shape(precision, nx, shape):

@@ -425,16 +425,19 @@ bool col_variant_built(int prec, int logny, int v)
 }
 
 namespace {
-// [precision][log2 Nx]: 0 radix 8, 1 radix 16 with stashes; seeded with radix 8
-std::atomic<int> g_rowv[3][LOG_MAX + 1] = {};
+// [precision][log2 Nx]: 0 lockstep radix 8, 1 in sequence with stashes; seeded
+// with 0, except double-float from Nx = 1024 (the lockstep kernel outgrows the
+// instruction caches there)
+std::atomic<int> g_rowv[3][LOG_MAX + 1] = {
+    {}, {}, {{0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {1}, {1}, {1}}};
 }  // namespace
 
 int row_variant(int prec, int lognx) { return g_rowv[pidx(prec)][lognx].load(std::memory_order_relaxed); }
 void set_row_variant(int prec, int lognx, int v) { g_rowv[pidx(prec)][lognx].store(v); }
-// Radix 16 with stashes: FP32, Nx >= 1024.
+// In sequence with stashes: FP32 and double-float, Nx >= 1024.
 bool row_variant_built(int prec, int lognx, int v)
 {
-    return v == 0 || (v == 1 && prec == AM_FP32 && lognx >= ROWS_LOG_MIN && lognx <= LOG_MAX);
+    return v == 0 || (v == 1 && prec != AM_FP64 && lognx >= ROWS_LOG_MIN && lognx <= LOG_MAX);
 }
 
 }  // namespace af

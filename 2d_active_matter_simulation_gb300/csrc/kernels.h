@@ -44,8 +44,8 @@ inline int col_grid(const LaunchShape &s, int ntp, int W) { return (ntp * W + s.
 
 // Column-pass launch shapes: 0 wide, 1 narrow, 2 wide radix 8 (FP32 only).
 constexpr int NCOLV = 3;
-// Row-pass launch shapes: 0 radix 8 in lockstep (RowPass), 1 radix 16 with
-// stashes (RowPassS; FP32, Nx >= 512).
+// Row-pass launch shapes: 0 radix 8 in lockstep (RowPass), 1 in sequence with
+// stashes (RowPassS; FP32 radix 16, double-float radix 8; Nx >= 512).
 constexpr int NROWV = 2;
 constexpr int ROWS_LOG_MIN = 10;   // RowPassS needs Nx >= 512 (log2 9); it is built from 1024 up
 
@@ -113,7 +113,7 @@ int col_variant(int prec, int logny);
 void set_col_variant(int prec, int logny, int v);
 bool col_variant_built(int prec, int logny, int v);
 // Row-pass launch shape for new simulations of this precision and log2 Nx
-// (0 radix 8, 1 radix 16 with stashes), as col_variant.
+// (0 lockstep, 1 in sequence with stashes), as col_variant.
 int row_variant(int prec, int lognx);
 void set_row_variant(int prec, int lognx, int v);
 bool row_variant_built(int prec, int lognx, int v);

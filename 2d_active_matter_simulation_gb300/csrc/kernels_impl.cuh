@@ -109,7 +109,9 @@ struct Fill {
     {
         t.row[LOG][0] = k_row<T, LOG>;
         t.row_shape[LOG][0] = {RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::smem_bytes(), RowKernel<T, LOG>::ROWS};
-        if constexpr (sizeof(T) == 4 && LOG >= ROWS_LOG_MIN) {   // radix-16 row shape: FP32, Nx >= 1024
+        // row shape 1, transforms in sequence: FP32 (radix 16) and
+        // double-float (radix 8), Nx >= 1024
+        if constexpr ((sizeof(T) == 4 || std::is_same_v<T, df>) && LOG >= ROWS_LOG_MIN) {
             t.row[LOG][1] = k_rows<T, LOG>;
             t.row_shape[LOG][1] = {RowPassS<T, LOG>::THREADS, RowPassS<T, LOG>::smem_bytes(), RowPassS<T, LOG>::ROWS};
         }

@@ -466,22 +466,30 @@ struct RowPass {
 template <typename T, int LOGNX>
 using RowKernel = RowPass<T, LOGNX>;
 
-// ----------------------------------------------- row pass, radix-16 shape
-// The same work as RowPass with radix-16 passes: TPC = M/16 threads per row
-// (64 at Nx = 2048), two exchanges per 1024-point transform instead of three,
-// and the transforms one after another instead of in lockstep: uy and ux,
-// once transformed, wait in two shared-memory stash buffers while w is
-// transformed (Q waits there while P is transformed), so each thread holds one
-// transform's 16 values at a time and the registers stay within 128.  Shared
-// memory per row: one exchange buffer (idx + idx/16 slots, the map of the
-// one-column radix-16 column pass) and the two stashes; the forward
-// transforms' pairing of Z(k) with Z(M-k) reads the stash that is free by
-// then.  FP32, Nx = 512 .. 4096.  Launch as RowPass.
+// ------------------------------------- row pass, transforms in sequence
+// The same work as RowPass with the transforms one after another instead of
+// in lockstep: uy and ux, once transformed, wait in two shared-memory stash
+// buffers while w is transformed (Q waits there while P is transformed), so
+// each thread holds one transform's values at a time.  Shared memory per row:
+// one exchange buffer and the two stashes; the forward transforms' pairing of
+// Z(k) with Z(M-k) reads the stash that is free by then.  Launch as RowPass.
+//  * FP32: radix-16 passes, TPC = M/16 threads per row (64 at Nx = 2048), two
+//    exchanges per 1024-point transform instead of three, registers within
+//    128; exchange slots idx + idx/16 (the map of the one-column radix-16
+//    column pass).  The transform loops are unrolled.
+//  * double-float: radix-8 passes, TPC = M/8 (128 at Nx = 2048), slots
+//    idx + idx/8, and the transform loops NOT unrolled, so one inverse and one
+//    forward transform are in the code instead of five: the lockstep kernel,
+//    fully unrolled, outgrows the instruction caches (ncu at 2048^2: 5.4
+//    no-instruction stall cycles per issue, 27% issue) and with 255 registers
+//    and 110 KB of exchange buffers per CTA keeps 8 warps per SM.
+// Nx = 512 .. 4096 (built from 1024).
 template <typename T, int LOGNX>
 struct RowPassS {
     static constexpr int M = 1 << (LOGNX - 1);
     static constexpr int LOGM = LOGNX - 1;
-    static constexpr int LOGR = 4;
+    static constexpr bool F32 = sizeof(T) == 4;
+    static constexpr int LOGR = F32 ? 4 : 3;
     using FFTi = BlockFFT<T, LOGM, LOGR, +1>;
     using FFTf = BlockFFT<T, LOGM, LOGR, -1>;
     static constexpr int R = FFTi::R;
@@ -489,8 +497,8 @@ struct RowPassS {
     static_assert(TPC >= 16 && TPC % Tile<T>::W == 0, "RowPassS: Nx >= 512");
     static constexpr int ROWS = TPC >= 128 ? 1 : 128 / TPC;
     static constexpr int THREADS = ROWS * TPC;
-    static constexpr int MINB = 4;
-    using Buf = XBuf<T, 1, 3>;
+    static constexpr int MINB = F32 || THREADS < 256 ? 4 : 2;   // 128 registers per thread at most
+    using Buf = XBuf<T, 1, F32 ? 3 : 0>;
     static constexpr int BUFS = (Buf::slots(M) + 7) / 8 * 8;
     static constexpr int SLOTS = BUFS + 2 * M;    // exchange + two stashes (complex values)
     static constexpr int NW = TPC / 32 > 0 ? TPC / 32 : 1;   // warps per row
@@ -551,7 +559,7 @@ struct RowPassS {
     template <class Sync>
     static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync)
     {
-        static_assert(R == 16, "radix-16 shape");
+        static_assert(R == (F32 ? 16 : 8), "radix 16 (FP32) / 8 (double-float)");
         const int rl = tid / TPC, j = tid % TPC;
         const int yy = bid * ROWS + rl;
         const bool active = yy < a.ny;
@@ -566,16 +574,16 @@ struct RowPassS {
 
         // ---- C2R along x of uy and ux (stashed), then w (kept in registers)
         cpx<T> v[R];
-        load_pack(v, a.fy, j, y, ny, a.kxp, wj);
-        FFTi::run(v, j, 0, xb, a.twx, 2, sync);
+#pragma unroll(F32 ? 3 : 1)
+        for (int f = 0; f < 3; f++) {
+            load_pack(v, f == 0 ? a.fy : f == 1 ? a.fx : a.fa, j, y, ny, a.kxp, wj);
+            FFTi::run(v, j, 0, xb, a.twx, 2, sync);
+            if (f < 2) {
+                cpx<T> *st = f == 0 ? s1 : s2;
 #pragma unroll
-        for (int r = 0; r < R; r++) s1[j + r * TPC] = v[r];
-        load_pack(v, a.fx, j, y, ny, a.kxp, wj);
-        FFTi::run(v, j, 0, xb, a.twx, 2, sync);
-#pragma unroll
-        for (int r = 0; r < R; r++) s2[j + r * TPC] = v[r];
-        load_pack(v, a.fa, j, y, ny, a.kxp, wj);
-        FFTi::run(v, j, 0, xb, a.twx, 2, sync);
+                for (int r = 0; r < R; r++) st[j + r * TPC] = v[r];
+            }
+        }
 
         // ---- real-space products (each thread reads and writes only its own
         // stash slots): P to v, Q to s1
@@ -605,12 +613,17 @@ struct RowPassS {
         // ---- R2C along x of P (pairing through s2, free since the products)
         // and of Q (pairing through s1, which each thread has read back)
         const int kend = a.ntp * Tile<T>::W;   // the column pass reads kx < kend
-        FFTf::run(v, j, 0, xb, a.twx, 2, sync);
-        unpack_store(v, s2, a.P, j, y, ny, kend, active, wj, sync);
+#pragma unroll(F32 ? 2 : 1)
+        for (int f = 0; f < 2; f++) {
+            if (f == 1) {
 #pragma unroll
-        for (int r = 0; r < R; r++) v[r] = s1[j + r * TPC];
-        FFTf::run(v, j, 0, xb, a.twx, 2, sync);   // its entry barrier orders the reads of s1 before the writes
-        unpack_store(v, s1, a.Q, j, y, ny, kend, active, wj, sync);
+                for (int r = 0; r < R; r++) v[r] = s1[j + r * TPC];
+            }
+            // (Q: the transform's entry barrier orders the reads of s1 before
+            // unpack_store's writes to it)
+            FFTf::run(v, j, 0, xb, a.twx, 2, sync);
+            unpack_store(v, f == 0 ? s2 : s1, f == 0 ? a.P : a.Q, j, y, ny, kend, active, wj, sync);
+        }
     }
 
     // Sum (t0, t1, t2) over the TPC threads of a row; valid in thread j = 0.

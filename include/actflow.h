@@ -312,14 +312,16 @@ long long am_footprint_bytes(const am_params *p);
  * (cuFFT picks its own plans, ActFlow_V3-2.cu:507-508). */
 am_status am_set_column_shape(int precision, int ny, int shape);
 int am_column_shape(int precision, int ny);   /* -1 for an unsupported size */
-/* The row pass has two launch shapes: 0 (radix-8 passes, 128 threads per
- * 2048-point row, the three inverse transforms in lockstep) and 1 (FP32,
- * Nx >= 1024: radix-16 passes, one exchange fewer per transform, half the
- * threads per row, the transforms one after another with two shared-memory
- * stashes).  One choice per (precision, Nx), seeded with shape 0, used by
- * every handle, batch and ragged batch created afterwards; AM_ERR_UNSUPPORTED
- * for a shape not built for the precision and Nx.  No counterpart in the
- * reference. */
+/* The row pass has two launch shapes: 0 "lockstep" (radix-8 passes, 128
+ * threads per 2048-point row, the three inverse transforms in lockstep) and 1
+ * "sequence" (FP32 and double-float, Nx >= 1024: the transforms one after
+ * another with two shared-memory stashes; FP32 with radix-16 passes, one
+ * exchange fewer per transform and half the threads per row; double-float
+ * with radix-8 passes and the transforms in a loop, a kernel small enough for
+ * the instruction caches).  One choice per (precision, Nx), seeded with shape
+ * 0 (double-float from Nx = 1024: shape 1), used by every handle, batch and
+ * ragged batch created afterwards; AM_ERR_UNSUPPORTED for a shape not built
+ * for the precision and Nx.  No counterpart in the reference. */
 am_status am_set_row_shape(int precision, int nx, int shape);
 int am_row_shape(int precision, int nx);      /* -1 for an unsupported size */
 /* Autotune: on the current device (a temporary handle with a seeded

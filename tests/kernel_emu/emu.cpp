@@ -106,8 +106,8 @@ struct Runner {
             }
         };
         auto row = [&]() {
-            if constexpr (sizeof(T) == 4 && LX >= ROWS_LOG_MIN) {
-                if (rowvar == 1) {   // radix-16 row shape with stashes
+            if constexpr ((sizeof(T) == 4 || std::is_same_v<T, df>) && LX >= ROWS_LOG_MIN) {
+                if (rowvar == 1) {   // row shape with the transforms in sequence (stashes)
                     using RS = RowPassS<T, LX>;
                     launch((ny + RS::ROWS - 1) / RS::ROWS, RS::THREADS, RS::smem_bytes(),
                            [&](int tid, int bid, unsigned char *sm, auto &sync) { RS::body(a, tid, bid, sm, sync); });
@@ -314,7 +314,7 @@ static int dispatch_all(const Call &c)
 // Advance (w_hat [ny][nx/2+1] complex of the precision, mean[2]) nsteps steps
 // with column-pass shape colvar (2: radix 8, FP32, column lengths 128, 1024,
 // 2048; otherwise the default for the length) and row-pass shape rowvar (0
-// radix 8, 1 radix 16 with stashes: FP32, Nx >= 1024).
+// lockstep, 1 in sequence with stashes: FP32 and double-float, Nx >= 1024).
 // Returns the first NaN step or -1; -100 for an unsupported size (8..128 each,
 // or one side 512..4096 with the other 8..16; double-float, w_hat in double:
 // 32x32, 64x64, 128x32, 2048x8, 8x2048).

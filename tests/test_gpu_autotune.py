@@ -48,9 +48,9 @@ def test_row_shapes_agree(am, nx, ny):
     """Both row-pass shapes give the same step (FP32, 1e-6)."""
     old = am.row_shape("fp32", nx)
     try:
-        am.set_row_shape("fp32", nx, "radix8")
+        am.set_row_shape("fp32", nx, "lockstep")
         w8, m8, e8 = _run(am, nx, ny, "fp32", am.column_shape("fp32", ny))
-        am.set_row_shape("fp32", nx, "radix16")
+        am.set_row_shape("fp32", nx, "sequence")
         w16, m16, e16 = _run(am, nx, ny, "fp32", am.column_shape("fp32", ny))
     finally:
         am.set_row_shape("fp32", nx, old)
@@ -65,7 +65,7 @@ def test_autotune_row_shape_at_2048(am):
     oc, orr = am.column_shape("fp32", 256), am.row_shape("fp32", 2048)
     try:
         _, _, rtimes, rchosen = am.autotune(p, nsteps=5)
-        assert set(rtimes) == {"radix8", "radix16"} and rchosen == min(rtimes, key=rtimes.get)
+        assert set(rtimes) == {"lockstep", "sequence"} and rchosen == min(rtimes, key=rtimes.get)
     finally:
         am.set_column_shape("fp32", 256, oc)
         am.set_row_shape("fp32", 2048, orr)
@@ -84,7 +84,7 @@ def test_autotune_keeps_the_faster_shape(am):
         times, chosen, rtimes, rchosen = am.autotune(p, nsteps=10)
         assert set(times) == {"wide", "narrow", "wide8"} and min(times.values()) > 0
         assert chosen == min(times, key=times.get)
-        assert set(rtimes) == {"radix8"} and rchosen == "radix8"   # radix 16 is built from Nx = 1024
+        assert set(rtimes) == {"lockstep"} and rchosen == "lockstep"   # the sequence shape is built from Nx = 1024
         # a batch created now uses the chosen shape and still matches a lone handle
         b = am.Batch([p, p])
         w0 = am.ic_bandlimited(512, 512, 5, rms=0.5).astype(np.complex64)
@@ -109,16 +109,33 @@ def test_autotune_keeps_the_faster_shape(am):
         am.set_column_shape("fp32", 512, old)
 
 
-def test_double_float_has_one_column_shape_per_length(am):
+def test_double_float_shapes(am):
     """Double-float builds the seeded column shape of each length only
-    (narrow below Ny = 2048, wide from it); the autotuner times that one and
-    the radix-8 row shape."""
+    (narrow below Ny = 2048, wide from it) and both row shapes from Nx = 1024
+    (seeded with the sequence shape there); the autotuner times what is
+    built, and the two row shapes agree."""
     with pytest.raises(am.ActflowError):
         am.set_column_shape("df64", 2048, "narrow")
     with pytest.raises(am.ActflowError):
-        am.set_row_shape("df64", 2048, "radix16")
-    p = am.make_params(512, 2048, 2 * math.pi, 2 * math.pi, 2e-4, 3.5, -0.8, 0.01, gamma0=-0.045,
+        am.set_row_shape("df64", 512, "sequence")
+    assert am.row_shape("df64", 2048) == "sequence" and am.row_shape("df64", 512) == "lockstep"
+    p = am.make_params(2048, 2048, 2 * math.pi, 2 * math.pi, 2e-4, 3.5, -0.8, 0.01, gamma0=-0.045,
                        gamma2=2.5e-5, dealias="half", precision="df64")
-    times, chosen, rtimes, rchosen = am.autotune(p, nsteps=3)
-    assert set(times) == {"wide"} and chosen == "wide" and times["wide"] > 0
-    assert set(rtimes) == {"radix8"} and rchosen == "radix8"
+    old = am.row_shape("df64", 2048)
+    try:
+        times, chosen, rtimes, rchosen = am.autotune(p, nsteps=3)
+        assert set(times) == {"wide"} and chosen == "wide" and times["wide"] > 0
+        assert set(rtimes) == {"lockstep", "sequence"} and rchosen == min(rtimes, key=rtimes.get)
+        w0 = am.ic_bandlimited(2048, 2048, 5, rms=0.5)
+        res = {}
+        for shape in ("lockstep", "sequence"):
+            am.set_row_shape("df64", 2048, shape)
+            sim = am.Solver(2048, 2048, p.lx, p.ly, p.dt, p.lam, p.alpha, p.beta, gamma0=p.gamma0,
+                            gamma2=p.gamma2, dealias="half", precision="df64")
+            sim.set_state(w0)
+            sim.step(4)
+            res[shape] = sim.get_state()[0]
+            sim.close()
+        assert np.linalg.norm(res["sequence"] - res["lockstep"]) / np.linalg.norm(res["lockstep"]) < 1e-13
+    finally:
+        am.set_row_shape("df64", 2048, old)

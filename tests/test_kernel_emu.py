@@ -224,17 +224,19 @@ def test_inside_half_mask_check(am, emu, n, prec):
         assert emu.emu_inside_half(ctypes.byref(p), v.ctypes.data) == 0, (iy, ix)
 
 
-@pytest.mark.parametrize("n,dealias", [((32, 32), "reference"), ((64, 64), "half"), ((128, 32), "none"),
-                                       ((2048, 8), "half"), ((8, 2048), "half")])
-def test_emulated_double_float(am, orc, emu, n, dealias):
+@pytest.mark.parametrize("n,dealias,rowvar", [((32, 32), "reference", 0), ((64, 64), "half", 0),
+                                              ((128, 32), "none", 0), ((2048, 8), "half", 0),
+                                              ((2048, 8), "half", 1), ((8, 2048), "half", 0)])
+def test_emulated_double_float(am, orc, emu, n, dealias, rowvar):
     """The double-float kernels (AM_DF64: two floats per real, FP32 arithmetic
-    only) against the FP64 oracle.  Double-float carries about 48 bits against
-    double's 53; the state agrees to about 5e-15 of its norm (FP32 would be off
-    by 1e-7)."""
+    only) against the FP64 oracle, with both row shapes at Nx = 2048 (rowvar 1:
+    the transforms in sequence, radix 8).  Double-float carries about 48 bits
+    against double's 53; the state agrees to about 5e-15 of its norm (FP32
+    would be off by 1e-7)."""
     nx, ny = n
     w0 = np.fft.rfft2(np.random.default_rng(nx + 3 * ny).standard_normal((ny, nx)))
     p = am.Params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, -0.045, 2.5e-5, 1, am.DEALIAS[dealias], am.DF64)
-    w, m, e = _emu_run(am, emu, p, w0, (3.0, 1.0), 3)
+    w, m, e = _emu_run(am, emu, p, w0, (3.0, 1.0), 3, rowvar=rowvar)
     op = orc.make_params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, -0.045, 2.5e-5, dealias=dealias,
                          if_double=True)
     wo, mo, eo = orc.run(op, w0, (3.0, 1.0), 3, "f64")

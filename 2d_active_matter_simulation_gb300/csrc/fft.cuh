@@ -450,6 +450,69 @@ struct BlockFFT {
 
     static constexpr int ipow(int b, int p) { return p == 0 ? 1 : b * ipow(b, p - 1); }
 
+    // The same transform with one buffer (as run(v, j, c, buf, ...)), in a
+    // compact form: the radix-R passes are a loop that is not unrolled (one
+    // pass body in the code instead of NPASS), and the inverse transform is
+    // the forward one between conjugations (conj F(conj x)), so both
+    // directions share that body's shape.  For arithmetic whose operations
+    // expand to many instructions (double-float), where the unrolled
+    // transforms outgrow the instruction caches.
+    template <class Buf, class Sync>
+    static AF_HD void run_compact(cpx<T> (&v)[R], int j, int c, const Buf &b, const cpx<T> *tw, int TWS,
+                                  Sync &&sync)
+    {
+        if constexpr (SIGN > 0) {
+#pragma unroll
+            for (int r = 0; r < R; r++) v[r] = conj(v[r]);
+        }
+        if constexpr (NEXCH > 0) sync();
+        bool in_buf = false;   // this pass's input is in the buffer (else in registers)
+        if constexpr (LOGR1 > 0) {
+            constexpr int G = R / R1;
+#pragma unroll
+            for (int q = 0; q < G; q++) {
+                cpx<T> u[R1];
+#pragma unroll
+                for (int r1 = 0; r1 < R1; r1++) u[r1] = v[q + G * r1];
+                DFT<R1, -1, T>::run(u);
+                const int base = (j + q * TPC) * R1;
+#pragma unroll
+                for (int r1 = 0; r1 < R1; r1++) b.put(base + r1, c, u[r1]);
+            }
+            sync();
+            in_buf = true;
+        }
+#pragma unroll 1
+        for (int p = 0; p < NPASS; p++) {
+            const int ns = R1 << (LOGR * p);   // sub-transform size of this pass
+            if (in_buf) {
+#pragma unroll
+                for (int r = 0; r < R; r++) v[r] = b.get(j + r * TPC, c);
+            }
+            if (ns > 1) {
+                const int k = j & (ns - 1);
+                cpx<T> w[R];
+                twiddles<R>(w, tw, (L / (ns * R)) * k * TWS);
+#pragma unroll
+                for (int r = 1; r < R; r++) v[r] = cmul(v[r], w[r]);
+            }
+            DFT<R, -1, T>::run(v);
+            if (p < NPASS - 1) {
+                const int k = j & (ns - 1);
+                const int base = (j - k) * R + k;
+                if (in_buf) sync();   // one buffer: this pass's reads must finish first
+#pragma unroll
+                for (int r = 0; r < R; r++) b.put(base + r * ns, c, v[r]);
+                sync();
+                in_buf = true;
+            }
+        }
+        if constexpr (SIGN > 0) {
+#pragma unroll
+            for (int r = 0; r < R; r++) v[r] = conj(v[r]);
+        }
+    }
+
     // NF transforms of the same length and direction in lockstep: v[f] holds
     // transform f (cyclic distribution), b0[f] / b1[f] are its two exchange
     // buffers.  The twiddles of a pass are formed once for all NF transforms

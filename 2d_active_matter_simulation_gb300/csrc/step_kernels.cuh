@@ -151,6 +151,15 @@ __device__ __forceinline__ df shfl_xor(df v, int o)
 }
 #endif
 
+// One-buffer block transform: the unrolled passes, or for double-float the
+// compact loop (BlockFFT::run_compact), whose code fits the instruction caches.
+template <class FFT, typename T, class Buf, class Sync>
+AF_HD void fft1(cpx<T> (&v)[FFT::R], int j, int c, const Buf &b, const cpx<T> *tw, int tws, Sync &&sync)
+{
+    if constexpr (std::is_same_v<T, df>) FFT::run_compact(v, j, c, b, tw, tws, sync);
+    else FFT::run(v, j, c, b, tw, tws, sync);
+}
+
 // ------------------------------------------------------------------ row pass
 // One row y per group of TPC threads; a complex FFT of length M = Nx/2 per
 // real transform (the half-length real-FFT construction).  The Hermitian pairs
@@ -577,7 +586,7 @@ struct RowPassS {
 #pragma unroll(F32 ? 3 : 1)
         for (int f = 0; f < 3; f++) {
             load_pack(v, f == 0 ? a.fy : f == 1 ? a.fx : a.fa, j, y, ny, a.kxp, wj);
-            FFTi::run(v, j, 0, xb, a.twx, 2, sync);
+            fft1<FFTi>(v, j, 0, xb, a.twx, 2, sync);
             if (f < 2) {
                 cpx<T> *st = f == 0 ? s1 : s2;
 #pragma unroll
@@ -621,7 +630,7 @@ struct RowPassS {
             }
             // (Q: the transform's entry barrier orders the reads of s1 before
             // unpack_store's writes to it)
-            FFTf::run(v, j, 0, xb, a.twx, 2, sync);
+            fft1<FFTf>(v, j, 0, xb, a.twx, 2, sync);
             unpack_store(v, f == 0 ? s2 : s1, f == 0 ? a.P : a.Q, j, y, ny, kend, active, wj, sync);
         }
     }
@@ -905,7 +914,7 @@ struct ColPass {
             cpx<T> ph[R], v[R];
 #pragma unroll
             for (int r = 0; r < R; r++) v[r] = active ? a.P[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
-            FFTf::run(v, j, c, buf, a.twy, 1, sync);
+            fft1<FFTf>(v, j, c, buf, a.twy, 1, sync);
 #pragma unroll
             for (int r = 0; r < R; r++) ph[r] = v[r];
 #pragma unroll
@@ -918,7 +927,7 @@ struct ColPass {
                     if constexpr (FFTf::NEXCH == 0) sync();
                 }
             }
-            FFTf::run(v, j, c, buf, a.twy, 1, sync);
+            fft1<FFTf>(v, j, c, buf, a.twy, 1, sync);
             const ColMask cm(a.dealias, a.rsq, nx, ny, kx);
 #pragma unroll
             for (int r = 0; r < R; r++) {
@@ -1097,7 +1106,7 @@ struct ColPass {
                     if (owner && kx == 0 && iy == 0) v[r] = mk(f == 1 ? m0 : m1, (T)0);
                 }
             }
-            FFTi::run(v, j, c, buf, a.twy, 1, sync);
+            fft1<FFTi>(v, j, c, buf, a.twy, 1, sync);
             cpx<T> *dst = f == 0 ? a.fa : f == 1 ? a.fx : a.fy;
             if (active) {
 #pragma unroll

@@ -304,15 +304,24 @@ static void choose_pruning(am_handle *h, bool on)
 template <typename T>
 static am_status set_state_impl(am_handle *h, const void *w_hat, const double mean[2])
 {
-    choose_pruning<T>(h, state_inside_half_mask<HostT<T>>((const HostT<T> *)w_hat, h->p.nx, h->p.ny));
     const size_t bytes = (size_t)h->p.ny * h->nxh * sizeof(cpx<T>);
     CK(h, cudaMemcpyAsync(h->stage, w_hat, bytes, cudaMemcpyHostToDevice, h->stream));
     if constexpr (std::is_same_v<T, df>) df_from_double_async(h->stage, (size_t)2 * h->p.ny * h->nxh, h->stream);
-    table<T>().tile<<<1024, 256, 0, h->stream>>>((const cpx<T> *)h->stage, (cpx<T> *)h->u0, h->p.ny, h->nxh,
-                                                 h->nt);
-    CK(h, cudaGetLastError());
-    am_status st = reset_scalars(h, mean);
+    am_status st = reset_scalars(h, mean);   // (zeroes Scalars::outside)
     if (st) return st;
+    // Pruned transforms need a state that is zero outside the 1/2-rule
+    // ellipse: the tile kernel checks that on the device while it converts
+    // the layout, and the choice is made before the first column pass.
+    const bool half = h->p.dealias == AM_DEALIAS_HALF;
+    table<T>().tile<<<1024, 256, 0, h->stream>>>((const cpx<T> *)h->stage, (cpx<T> *)h->u0, h->p.ny, h->nxh,
+                                                 h->nt, h->p.nx, half ? &h->sc->outside : nullptr);
+    CK(h, cudaGetLastError());
+    int outside = 0;
+    if (half) {
+        CK(h, cudaMemcpyAsync(&outside, &h->sc->outside, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    choose_pruning<T>(h, half && outside == 0);
     st = launch_col<T>(h, 0);
     if (st) return st;
     CK(h, cudaStreamSynchronize(h->stream));

@@ -258,7 +258,7 @@ am_status am_batch_set_state(am_batch *b, int member, const void *w_hat, const d
     const KernelTable<float> &K = kernels_f32();
     StepArgs<float> &a = b->hargs[member];
     BK(cudaMemcpyAsync(b->stage, w_hat, bytes, cudaMemcpyHostToDevice, b->stream));
-    K.tile<<<1024, 256, 0, b->stream>>>(b->stage, a.u0, b->ny, b->nxh, b->nt);
+    K.tile<<<1024, 256, 0, b->stream>>>(b->stage, a.u0, b->ny, b->nxh, b->nt, b->nx, nullptr);
     BK(cudaGetLastError());
     Scalars s{};
     s.m_new[0] = s.m_old[0] = s.m_appr[0] = mean ? mean[0] : 0.0;

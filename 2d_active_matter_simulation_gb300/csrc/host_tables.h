@@ -4,6 +4,7 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <type_traits>
 #include <vector>
 
@@ -169,19 +170,38 @@ void set_pruning(StepArgs<T> &a, bool on)
 // The kept modes of a row form a prefix ix <= lim(iy) (mask_at's condition is
 // monotone in ix), so each row's limit is found once and only the entries past
 // it are tested.
-template <typename T>
-bool state_inside_half_mask(const T *w, int nx, int ny)
+// The entries past the limit are tested as bit patterns with each
+// component's sign bit cleared (zero for +0 and -0 only, as x != 0), OR-ed
+// over the row: a branch-free loop the compiler vectorises.  W is the word of
+// one real component (32 bits for float and for each half of a double-float,
+// 64 for double), per_cpx the words per complex value.  (The C ABI's
+// set_state does this check on the device, in the tile kernel.)
+template <typename W>
+bool inside_half_mask_bits(const void *w, int per_cpx, int nx, int ny)
 {
+    constexpr W MAG = ~(W(1) << (8 * sizeof(W) - 1));
+    const unsigned char *base = static_cast<const unsigned char *>(w);
     const int nxh = nx / 2 + 1;
     int lim = nxh - 1;   // kept ix of the row: 0..lim (lim = -1: none)
     for (int iy = 0; iy < ny; iy++) {
         while (lim >= 0 && !mask_at(1, 0, nx, ny, lim, iy)) lim--;
         while (lim + 1 < nxh && mask_at(1, 0, nx, ny, lim + 1, iy)) lim++;
-        const T *row = w + (size_t)iy * nxh * 2;
-        for (int k = 2 * (lim + 1); k < 2 * nxh; k++)
-            if (row[k] != 0) return false;
+        const unsigned char *row = base + (size_t)iy * nxh * per_cpx * sizeof(W);
+        W acc = 0;
+        for (int k = per_cpx * (lim + 1); k < per_cpx * nxh; k++) {
+            W b;
+            std::memcpy(&b, row + (size_t)k * sizeof(W), sizeof(W));
+            acc |= b & MAG;
+        }
+        if (acc != 0) return false;
     }
     return true;
+}
+template <typename T>
+bool state_inside_half_mask(const T *w, int nx, int ny)
+{
+    if constexpr (std::is_same_v<T, double>) return inside_half_mask_bits<uint64_t>(w, 2, nx, ny);
+    else return inside_half_mask_bits<uint32_t>(w, 2 * (int)(sizeof(T) / 4), nx, ny);   // float, double-float
 }
 
 }  // namespace af

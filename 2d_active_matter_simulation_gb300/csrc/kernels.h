@@ -59,7 +59,7 @@ struct KernelTable {
     LaunchShape rowfwd_shape[LOG_MAX + 1];
     void (*colfwd[LOG_MAX + 1])(const cpx<T> *, cpx<T> *, const cpx<T> *, int, int, int, int, int, int, int);
     LaunchShape colfwd_shape[LOG_MAX + 1];
-    void (*tile)(const cpx<T> *, cpx<T> *, int, int, int);    // [ny][nxh] -> tiled
+    void (*tile)(const cpx<T> *, cpx<T> *, int, int, int, int, int *);   // [ny][nxh] -> tiled
     void (*untile)(const cpx<T> *, cpx<T> *, int, int, int);  // tiled -> [ny][nxh]
     void (*lintab)(cpx<T> *, int, int, int, LinCoef);         // integrating-factor table
 };

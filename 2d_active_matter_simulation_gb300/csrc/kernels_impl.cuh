@@ -49,9 +49,12 @@ __global__ void __launch_bounds__(ColFwd<T, LOG>::THREADS)
                          []() { __syncthreads(); });
 }
 
-// Reference half-plane layout [ny][nxh] <-> tiled layout; padding columns zero.
+// Reference half-plane layout [ny][nxh] <-> tiled layout; padding columns
+// zero.  With `outside` non-null, sets *outside = 1 if the state has a nonzero
+// value at a mode the 1/2 rule removes (the device form of
+// state_inside_half_mask; every writer stores the same value).
 template <typename T>
-__global__ void k_tile(const cpx<T> *src, cpx<T> *dst, int ny, int nxh, int nt)
+__global__ void k_tile(const cpx<T> *src, cpx<T> *dst, int ny, int nxh, int nt, int nx, int *outside)
 {
     constexpr int W = Tile<T>::W;
     size_t total = (size_t)nt * W * ny;
@@ -61,7 +64,9 @@ __global__ void k_tile(const cpx<T> *src, cpx<T> *dst, int ny, int nxh, int nt)
         int y = (int)(rest % ny);
         int t = (int)(rest / ny);
         int kx = t * W + c;
-        dst[i] = kx < nxh ? src[(size_t)y * nxh + kx] : mk<T>(0, 0);
+        const cpx<T> v = kx < nxh ? src[(size_t)y * nxh + kx] : mk<T>(0, 0);
+        dst[i] = v;
+        if (outside && (v.x != T(0) || v.y != T(0)) && !mask_at(1, 0, nx, ny, kx, y)) *outside = 1;
     }
 }
 

@@ -197,7 +197,7 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
     k_tables<T><<<(nmax + 255) / 256, 256, 0, st>>>((cpx<T> *)a.twx, (cpx<T> *)a.twy, (T *)a.kxt, (T *)a.kyt, nx, ny,
                                                    nxh, nkx, (T)p.lx, (T)p.ly);
     k_mean<<<1, 1, 0, st>>>(a.sc, mean, 1);
-    K.tile<<<1024, 256, 0, st>>>((const cpx<T> *)w_hat, a.u0, ny, nxh, nt);
+    K.tile<<<1024, 256, 0, st>>>((const cpx<T> *)w_hat, a.u0, ny, nxh, nt, nx, nullptr);
     const int rgrid = (ny + rs.per_block - 1) / rs.per_block;
     const int cgrid = col_grid(cs, nt, Tile<T>::W);
     StepArgs<T> b = a;

@@ -461,7 +461,7 @@ am_status am_ragged_set_state(am_ragged *r, int run, const void *w_hat, const do
     const KernelTable<float> &K = kernels_f32();
     const size_t bytes = (size_t)R.p.ny * R.nxh * sizeof(cpx<float>);
     RK(cudaMemcpyAsync(r->stage, w_hat, bytes, cudaMemcpyHostToDevice, r->stream));
-    K.tile<<<1024, 256, 0, r->stream>>>(r->stage, R.a.u0, R.p.ny, R.nxh, R.nt);
+    K.tile<<<1024, 256, 0, r->stream>>>(r->stage, R.a.u0, R.p.ny, R.nxh, R.nt, R.p.nx, nullptr);
     RK(cudaGetLastError());
     Scalars s{};
     s.m_new[0] = s.m_old[0] = s.m_appr[0] = mean ? mean[0] : 0.0;

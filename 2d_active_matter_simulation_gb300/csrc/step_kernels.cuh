@@ -38,7 +38,8 @@ struct Scalars {
     int step;                              // steps completed since set_state
     int nan_step;                          // first step whose w(0,0) is NaN, or -1
     int status;                            // reserved device status word (0 = ok)
-    int pad_;
+    int outside;                           // set_state: the loaded state has a nonzero mode
+                                           // outside the 1/2-rule ellipse (tile kernel)
 };
 static_assert(sizeof(Scalars) == 64, "the column pass copies Scalars as four 16-byte pieces");
 

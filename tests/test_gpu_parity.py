@@ -296,3 +296,28 @@ def test_gpu_zero_steps_leave_the_state(am):
     assert res["status"] == am.AM_OK and res["steps_done"] == 0
     w9 = am.ic_bandlimited(128, 128, 9, 1.0, 8.0, 0.01).astype(np.complex64)
     assert np.array_equal(res["state"], w9)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64", "df64"])
+def test_gpu_pruning_choice_on_the_device(am, prec):
+    """set_state checks on the device, in the tile kernel, whether the state
+    is zero outside the 1/2-rule ellipse (pruned transforms) -- the same
+    decision as the host check: a negative zero outside still counts as zero,
+    one nonzero mode outside (or a NaN) turns pruning off."""
+    nx, ny = 256, 128
+    w0 = am.ic_bandlimited(nx, ny, seed=3, kmax=10.0, rms=1.0)
+    w0 = w0 if prec != "fp32" else w0.astype(np.complex64)
+    sim = am.Solver(nx, ny, 2 * math.pi, 2 * math.pi, 1e-4, 3.5, -0.8, 0.01, gamma0=-0.045, gamma2=2.5e-5,
+                    dealias="half", precision=prec)
+    sim.set_state(w0)
+    assert sim.kx_carried == nx // 4
+    w = w0.copy()
+    w[5, nx // 2 - 3] = complex(-0.0, -0.0)
+    sim.set_state(w)
+    assert sim.kx_carried == nx // 4
+    for val in (1e-30, complex(0.0, 2.0), complex(float("nan"), 0.0)):
+        w = w0.copy()
+        w[ny // 2, 3 * nx // 8] = val
+        sim.set_state(w)
+        assert sim.kx_carried == nx // 2, val
+    sim.close()

@@ -124,4 +124,43 @@ DF_HD df &operator*=(df &a, df b) { return a = a * b; }
 DF_HD bool operator!=(df a, df b) { return a.hi != b.hi || a.lo != b.lo; }   // a NaN differs from itself
 DF_HD bool operator==(df a, df b) { return !(a != b); }
 
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+// Two double-float numbers side by side -- the high parts in one float2, the
+// low parts in another -- for Blackwell's packed FP32x2 instructions: one
+// instruction carries both numbers' step of an operation.  Each lane rounds as
+// the scalar intrinsic does (a - b as fma(b, -1, a), whose product is exact),
+// so every operation below gives bit for bit the two scalar results.
+struct df2 {
+    float2 hi, lo;
+};
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ df2 df2_of(df a, df b) { return {make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)}; }
+__device__ __forceinline__ df df2_first(df2 v) { return df(v.hi.x, v.lo.x); }
+__device__ __forceinline__ df df2_second(df2 v) { return df(v.hi.y, v.lo.y); }
+__device__ __forceinline__ df2 df2_fast_two_sum(float2 a, float2 b)
+{
+    const float2 s = __fadd2_rn(a, b);
+    return {s, f2_sub(b, f2_sub(s, a))};
+}
+__device__ __forceinline__ df2 df2_two_sum(float2 a, float2 b)
+{
+    const float2 s = __fadd2_rn(a, b);
+    const float2 bb = f2_sub(s, a);
+    return {s, __fadd2_rn(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb))};
+}
+__device__ __forceinline__ df2 df2_add(df2 a, df2 b)
+{
+    const df2 s = df2_two_sum(a.hi, b.hi);
+    return df2_fast_two_sum(s.hi, __fadd2_rn(s.lo, __fadd2_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df2 df2_mul(df2 a, df2 b)
+{
+    const float2 p = __fmul2_rn(a.hi, b.hi);
+    float2 e = __ffma2_rn(a.hi, b.hi, make_float2(-p.x, -p.y));
+    e = __ffma2_rn(a.hi, b.lo, e);
+    e = __ffma2_rn(a.lo, b.hi, e);
+    return df2_fast_two_sum(p, e);
+}
+#endif
+
 }  // namespace af

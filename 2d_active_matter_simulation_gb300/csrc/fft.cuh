@@ -98,6 +98,31 @@ AF_HD cpx<float> cmulc(cpx<float> a, cpx<float> b)
     return mk(r.x, r.y);
 }
 #endif
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+// Double-float complex arithmetic on the packed FP32x2 pipe: the real and
+// imaginary parts go through identical operation sequences, run side by side
+// (df2, dfloat.cuh) -- half the instructions, bit-identical results to the
+// scalar double-float forms (a - b is a + (-b) there, and negations are exact).
+AF_HD cpx<df> df2_cpx(df2 v) { return mk(df2_first(v), df2_second(v)); }
+template <>
+AF_HD cpx<df> operator+(cpx<df> a, cpx<df> b) { return df2_cpx(df2_add(df2_of(a.x, a.y), df2_of(b.x, b.y))); }
+template <>
+AF_HD cpx<df> operator-(cpx<df> a, cpx<df> b) { return df2_cpx(df2_add(df2_of(a.x, a.y), df2_of(-b.x, -b.y))); }
+template <>
+AF_HD cpx<df> cmul(cpx<df> a, cpx<df> b)
+{
+    const df2 t = df2_mul(df2_of(a.x, a.x), df2_of(b.x, b.y));
+    const df2 u = df2_mul(df2_of(a.y, a.y), df2_of(-b.y, b.x));
+    return df2_cpx(df2_add(t, u));
+}
+template <>
+AF_HD cpx<df> cmulc(cpx<df> a, cpx<df> b)
+{
+    const df2 t = df2_mul(df2_of(a.x, a.y), df2_of(b.x, b.x));
+    const df2 u = df2_mul(df2_of(a.y, a.x), df2_of(b.y, -b.y));
+    return df2_cpx(df2_add(t, u));
+}
+#endif
 template <typename T>
 AF_HD cpx<T> conj(cpx<T> a) { return mk(a.x, -a.y); }
 template <typename T>
@@ -109,6 +134,8 @@ AF_HD cpx<float> scale(cpx<float> a, float s)
     const float2 r = __fmul2_rn(make_float2(a.x, a.y), make_float2(s, s));
     return mk(r.x, r.y);
 }
+template <>
+AF_HD cpx<df> scale(cpx<df> a, df s) { return df2_cpx(df2_mul(df2_of(a.x, a.y), df2_of(s, s))); }
 #endif
 
 // Multiply by exp(SIGN * 2 pi i Q / R) for compile-time Q, R (R <= 32).
@@ -150,6 +177,7 @@ AF_HD cpx<T> rot(cpx<T> a)
             const float2 r = __ffma2_rn(make_float2(a.y, a.y), make_float2(-s, c), t);
             return mk(r.x, r.y);
         }
+        if constexpr (std::is_same_v<T, df>) return cmul(a, mk(c, s));   // packed double-float
 #endif
         return mk(a.x * c - a.y * s, a.x * s + a.y * c);
     }

@@ -321,3 +321,25 @@ def test_gpu_pruning_choice_on_the_device(am, prec):
         sim.set_state(w)
         assert sim.kx_carried == nx // 2, val
     sim.close()
+
+
+@pytest.mark.parametrize("if_factors", ["float", "double"])
+def test_gpu_double_float_integrating_factor_forms(am, orc, if_factors):
+    """Double-float with the integrating factors per value (exp in double on
+    the device, split once) and from the double table: both against the FP64
+    oracle, which forms them in double."""
+    n = 128
+    w0 = am.ic_bandlimited(n, n, seed=31, kmin=1, kmax=20, rms=5.0)
+    mean0 = (0.05 * n * n, -0.02 * n * n)
+    sim = am.Solver(n, n, 2 * math.pi, 2 * math.pi, 2e-4, 3.5, -0.8, 0.01, gamma0=-0.045, gamma2=2.5e-5,
+                    dealias="half", precision="df64", if_factors=if_factors)
+    sim.set_state(w0, mean0)
+    e = sim.step(20)
+    w, m = sim.get_state()
+    sim.close()
+    p = orc.make_params(n, n, 2 * math.pi, 2 * math.pi, 2e-4, 3.5, -0.8, 0.01, -0.045, 2.5e-5, dealias="half",
+                        if_double=if_factors == "double")
+    wo, mo, eo = orc.run(p, w0, mean0, 20, "f64")
+    assert rel(w, wo) < 1e-11
+    assert np.abs(e - eo).max() <= 1e-11 * np.abs(eo).max()
+    assert np.abs(m - mo).max() <= 1e-11 * np.abs(mo).max()

@@ -475,6 +475,30 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
 
 
+def run_profile_case(args):
+    """The workload's step, untimed, for profilers: the seeded field loaded
+    with the launch shapes given (no autotuning), then args.steps steps.  The
+    kernels run in the order set-up column pass, then (row pass, column pass
+    stage s) for s = 1..4 per step."""
+    import importlib
+
+    import numpy as np
+
+    am = importlib.import_module("2d_active_matter_simulation_gb300")
+    col, row = args.profile_case.split(",")
+    am.set_column_shape(PRECISION, NY, col)
+    am.set_row_shape(PRECISION, NX, row)
+    sim = am.Solver(NX, NY, PARAMS["lx"], PARAMS["ly"], PARAMS["dt"], PARAMS["lam"], PARAMS["alpha"], PARAMS["beta"],
+                    gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"], precision=PRECISION)
+    w0 = am.ic_bandlimited(NX, NY, SEED)
+    sim.set_state(w0.astype(np.complex64) if PRECISION == "fp32" else w0, (0.0, 0.0))
+    e = sim.step(args.steps)
+    sim.close()
+    print(json.dumps({"profile_case": {"workload": WORKLOAD, "column_shape": col, "row_shape": row,
+                                       "steps": args.steps, "energy_last": float(e[-1]) if len(e) else None}}),
+          flush=True)
+
+
 def precision_paths(am, stream, flush, nsteps):
     """ms per step of the FP64 and double-float paths on the headline workload
     (seeded field, default launch shapes, L2 flushed before every step) and
@@ -858,6 +882,9 @@ def main():
                     help="configs 0/1: grid size N (N x N) instead of the preset's, e.g. 4096 (fields exceed L2)")
     ap.add_argument("--serve-seconds", type=float, default=20.0, help="config 4: arrival window")
     ap.add_argument("--serve-step-scale", type=float, default=0.05, help="config 4: step-count scale")
+    ap.add_argument("--profile-case", metavar="COL,ROW", default="",
+                    help="configs 0/1: no timing; load the seeded field with the given column and row shapes "
+                         "(e.g. wide8,lockstep) and run --steps steps: a short, deterministic command for ncu")
     args = ap.parse_args()
     if args.impl == "ours":
         replica_setup()   # before torch or the solver touch a GPU
@@ -866,6 +893,11 @@ def main():
     apply_preset(args.config, args.precision, args.n or None)
     if args.accuracy:
         run_accuracy(args)
+        return
+    if args.profile_case:
+        if args.config not in (0, 1):
+            ap.error("--profile-case applies to configs 0 and 1")
+        run_profile_case(args)
         return
     if args.config in (2, 3, 4) and world()[1] != 0:
         return   # the ensemble, ragged and serving workloads run on one GPU (rank 0)

@@ -88,18 +88,35 @@ def test_cli_nan_exits_1(am, tmp_path):
     assert len(t) == 1
 
 
-def test_cli_fresh_bandlimited_fp64(am, tmp_path):
-    d = str(tmp_path)
+def _fresh_bandlimited(am, d, precision):
     write_spec(os.path.join(d, "specifications.txt"), [
         ("T", "0.01"), ("dt", "0.001"), ("Lx", "6.283185307"), ("Ly", "6.283185307"), ("Nx", 64), ("Ny", 64),
         ("lambda", "3.5"), ("alpha", "-0.8"), ("beta", "0.01"), ("dt_snap", "0.005"),
-        ("initial_condition", "bandlimited 42"), ("save_directory", d), ("precision", "fp64"),
+        ("initial_condition", "bandlimited 42"), ("save_directory", d), ("precision", precision),
         ("dealias", "half"), ("Gamma0", "-0.045"), ("Gamma2", "2.5e-5")])
     p = _run(am, d)
     assert p.returncode == 0, p.stderr
     t, e = read_energy(os.path.join(d, "energy.txt"))
     assert len(t) == 10 and abs(t[0] - 0.001) < 1e-9
     assert os.path.exists(os.path.join(d, "ActTurb_snap2.bin"))
+    return e, read_snapshot(os.path.join(d, "ActTurb_snap2.bin"), 64, 64)
+
+
+def test_cli_fresh_bandlimited_fp64(am, tmp_path):
+    _fresh_bandlimited(am, str(tmp_path), "fp64")
+
+
+def test_cli_double_float_matches_fp64(am, tmp_path):
+    """`precision: df64` through the drop-in program: the same files as an FP64
+    run, with energies and the snapshot (printed to six digits, as the
+    reference's text snapshots) equal to the FP64 run's up to rounding of
+    the last printed digit."""
+    os.makedirs(tmp_path / "a")
+    os.makedirs(tmp_path / "b")
+    e64, (w64, m64) = _fresh_bandlimited(am, str(tmp_path / "a"), "fp64")
+    edf, (wdf, mdf) = _fresh_bandlimited(am, str(tmp_path / "b"), "df64")
+    assert np.abs(edf - e64).max() <= 1e-5 * np.abs(e64).max()
+    assert np.abs(wdf - w64).max() <= 1e-5 * np.abs(w64).max()
 
 
 def _raw(path, nx, ny):

@@ -756,6 +756,15 @@ AF_HD void cp_async8(void *dst_smem, const void *src)
     for (int i = 0; i < 8; i++) static_cast<unsigned char *>(dst_smem)[i] = static_cast<const unsigned char *>(src)[i];
 #endif
 }
+// Hint to bring the line holding p into this SM's L1 (no register, no wait).
+AF_HD void prefetch_l1(const void *p)
+{
+#ifdef __CUDA_ARCH__
+    asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
+#else
+    (void)p;
+#endif
+}
 // Named barrier 1 (barrier 0 is __syncthreads): bar_arrive signals without
 // waiting, bar_wait waits until `n` threads have arrived or waited; prior
 // shared-memory writes of the arriving threads are visible after the wait.
@@ -920,6 +929,18 @@ struct ColPass {
             for (int r = 0; r < R; r++) ph[r] = v[r];
 #pragma unroll
             for (int r = 0; r < R; r++) v[r] = active ? a.Q[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
+            // the stage's inputs move towards L1 while Q is transformed
+            if (active) {
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    const size_t g = cbase + (size_t)(j + r * TPC) * W;
+                    if constexpr (MODE != 4) prefetch_l1(a.u0 + g);
+                    if constexpr (MODE >= 2) prefetch_l1(a.acc + g);
+                    if constexpr (MODE != 4) {
+                        if (a.lintab) prefetch_l1(a.lintab + g);
+                    }
+                }
+            }
             if constexpr (PS) {
                 // the owner's copies are complete; the barrier that starts the
                 // next transform makes them visible to the whole CTA

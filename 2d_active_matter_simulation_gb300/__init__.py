@@ -477,8 +477,9 @@ def column_shape(precision, ny):
 
 # row-pass shapes: the three inverse transforms in lockstep (radix 8), or one
 # after another with shared-memory stashes ("sequence": FP32 radix 16,
-# double-float radix 8; Nx >= 1024)
-ROW_SHAPES = ("lockstep", "sequence")
+# double-float radix 8; Nx >= 1024), or lockstep with the input rows fetched
+# by tensor-map copies ("lockstep-tma": FP32, Nx = 2048 and 4096)
+ROW_SHAPES = ("lockstep", "sequence", "lockstep-tma")
 
 
 def set_row_shape(precision, nx, shape):

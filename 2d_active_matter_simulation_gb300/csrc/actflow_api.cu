@@ -9,6 +9,7 @@
 // plus per-row sums, scalars, the energy ring and small tables.  A step is 8
 // kernel launches (row pass + column pass per RK stage), captured once into a
 // CUDA graph and replayed.
+#include <cuda.h>   // CUtensorMap and its encoder's types (the encoder is reached through the runtime)
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -67,6 +68,10 @@ struct am_handle {
     StepArgs<float> a32{};
     StepArgs<double> a64{};
     StepArgs<df> adf{};
+    // row shape 2 (FP32): tensor maps of the row pass's inputs for the current
+    // pruning, and whether a row's carried tiles fit its staging buffer
+    RowTma tma{};
+    bool tma_ok = false;
 };
 
 // Calls f with a value of the state type of precision prec: float (AM_FP32),
@@ -183,7 +188,9 @@ static am_status alloc_and_tables(am_handle *h)
     struct {
         const void *fn;
         size_t smem;
-    } ks[] = {{(const void *)K.row[h->lognx][h->rowv], K.row_shape[h->lognx][h->rowv].smem},
+    } ks[] = {{(const void *)K.row[h->lognx][h->rowv == ROWV_TMA ? 0 : h->rowv],
+               K.row_shape[h->lognx][h->rowv == ROWV_TMA ? 0 : h->rowv].smem},
+              {(const void *)K.row_tma[h->lognx], K.row_tma_shape[h->lognx].smem},
               {(const void *)K.col[h->logny][h->colv][0], K.col_shape[h->logny][h->colv].smem},
               {(const void *)K.col[h->logny][h->colv][1], K.col_shape[h->logny][h->colv].smem},
               {(const void *)K.col[h->logny][h->colv][2], K.col_shape[h->logny][h->colv].smem},
@@ -192,10 +199,68 @@ static am_status alloc_and_tables(am_handle *h)
               {(const void *)K.rowfwd[h->lognx], K.rowfwd_shape[h->lognx].smem},
               {(const void *)K.colfwd[h->logny], K.colfwd_shape[h->logny].smem}};
     for (auto &k : ks) {
-        if (k.smem > 48 * 1024)
+        if (k.fn && k.smem > 48 * 1024)
             CK(h, cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem));
     }
     return AM_OK;
+}
+
+// cuTensorMapEncodeTiled from the driver, found through the runtime (the
+// library links no driver library of its own).
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiled encode_tiled()
+{
+    static EncodeTiled fn = []() -> EncodeTiled {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return reinterpret_cast<EncodeTiled>(p);
+    }();
+    return fn;
+}
+
+// Tensor maps of the FP32 row pass's three inputs (fy, fx, fa) for the
+// handle's current pruning: each field as {8 floats of a tile row, Ny rows,
+// column tiles}, boxes of one row and `box` tiles, nbox boxes per row covering
+// the ntp carried tiles (a box may run past them: those tiles are read and
+// never used).  tma_ok only where those tiles fit one exchange
+// buffer of the row pass (else row shape 2 runs as shape 0).
+static void prepare_row_tma(am_handle *h)
+{
+    h->tma_ok = false;
+    if (h->prec != AM_FP32 || h->rowv != ROWV_TMA) return;
+    const KernelTable<float> &K = kernels_f32();
+    const StepArgs<float> &a = h->a32;
+    if (!K.row_tma[h->lognx]) return;
+    const int W = Tile<float>::W;
+    // boxes of a multiple of 4 tiles (128 bytes), so that every box lands on
+    // a 128-byte boundary of the staging buffer
+    const int nbox = (a.ntp + 255) / 256, box = ((a.ntp + nbox - 1) / nbox + 3) / 4 * 4;
+    if (nbox * box * W > K.row_tma_cap[h->lognx]) return;
+    EncodeTiled enc = encode_tiled();
+    if (!enc) return;
+    static_assert(sizeof(CUtensorMap) == sizeof(TmaDesc) && alignof(TmaDesc) >= alignof(CUtensorMap),
+                  "TmaDesc holds a CUtensorMap");
+    const cuuint64_t dims[3] = {(cuuint64_t)(2 * W), (cuuint64_t)h->p.ny, (cuuint64_t)h->nt};
+    const cuuint64_t strides[2] = {(cuuint64_t)(2 * W) * sizeof(float), (cuuint64_t)h->p.ny * 2 * W * sizeof(float)};
+    const cuuint32_t boxd[3] = {(cuuint32_t)(2 * W), 1, (cuuint32_t)box};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    void *fields[3] = {h->fy, h->fx, h->fa};
+    for (int f = 0; f < 3; f++) {
+        CUresult r = enc(reinterpret_cast<CUtensorMap *>(&h->tma.map[f]), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                         fields[f], dims, strides, boxd, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return;
+    }
+    h->tma.nbox = nbox;
+    h->tma.box = box;
+    h->tma_ok = true;
 }
 
 template <typename T>
@@ -215,9 +280,22 @@ template <typename T>
 static am_status launch_row(am_handle *h)
 {
     const KernelTable<T> &K = table<T>();
-    const LaunchShape &s = K.row_shape[h->lognx][h->rowv];
+    if (h->rowv == ROWV_TMA) {
+        if constexpr (std::is_same_v<T, float>) {
+            prepare_row_tma(h);
+            if (h->tma_ok) {
+                const LaunchShape &s = K.row_tma_shape[h->lognx];
+                int grid = (h->p.ny + s.per_block - 1) / s.per_block;
+                K.row_tma[h->lognx]<<<grid, s.threads, s.smem, h->stream>>>(args_of<T>(h), h->tma);
+                CK(h, cudaGetLastError());
+                return AM_OK;
+            }
+        }
+    }
+    const int v = h->rowv == ROWV_TMA ? 0 : h->rowv;   // shape 2 without usable maps runs as shape 0
+    const LaunchShape &s = K.row_shape[h->lognx][v];
     int grid = (h->p.ny + s.per_block - 1) / s.per_block;
-    K.row[h->lognx][h->rowv]<<<grid, s.threads, s.smem, h->stream>>>(args_of<T>(h));
+    K.row[h->lognx][v]<<<grid, s.threads, s.smem, h->stream>>>(args_of<T>(h));
     CK(h, cudaGetLastError());
     return AM_OK;
 }
@@ -402,6 +480,10 @@ static am_status step_impl(am_handle *h, int nsteps, double *energy, int *nan_st
             h->err = "w(0,0) is NaN after step " + std::to_string(done + s.nan_step);
             return AM_ERR_NAN;
         }
+        if (s.status != 0) {
+            h->err = "a row pass's tensor-map copies did not complete in time";
+            return AM_ERR_TIMEOUT;
+        }
         done += k;
     }
     return AM_OK;
@@ -443,9 +525,11 @@ std::atomic<int> g_rowv[3][LOG_MAX + 1] = {
 
 int row_variant(int prec, int lognx) { return g_rowv[pidx(prec)][lognx].load(std::memory_order_relaxed); }
 void set_row_variant(int prec, int lognx, int v) { g_rowv[pidx(prec)][lognx].store(v); }
-// In sequence with stashes: FP32 and double-float, Nx >= 1024.
+// In sequence with stashes: FP32 and double-float, Nx >= 1024.  Tensor-map
+// row fetches: FP32, Nx = 2048 and 4096 (one row per CTA).
 bool row_variant_built(int prec, int lognx, int v)
 {
+    if (v == ROWV_TMA) return prec == AM_FP32 && (lognx == 11 || lognx == 12);
     return v == 0 || (v == 1 && prec != AM_FP64 && lognx >= ROWS_LOG_MIN && lognx <= LOG_MAX);
 }
 
@@ -474,10 +558,14 @@ template <typename T>
 static am_status use_row_variant(am_handle *h, int v)
 {
     const KernelTable<T> &K = table<T>();
-    const LaunchShape &rs = K.row_shape[h->lognx][v];
+    const int v0 = v == ROWV_TMA ? 0 : v;   // shape 2 falls back to shape 0's kernel
+    const LaunchShape &rs = K.row_shape[h->lognx][v0];
     if (rs.smem > 48 * 1024)
-        CK(h, cudaFuncSetAttribute((const void *)K.row[h->lognx][v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+        CK(h, cudaFuncSetAttribute((const void *)K.row[h->lognx][v0], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)rs.smem));
+    if (v == ROWV_TMA && K.row_tma[h->lognx] && K.row_tma_shape[h->lognx].smem > 48 * 1024)
+        CK(h, cudaFuncSetAttribute((const void *)K.row_tma[h->lognx], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)K.row_tma_shape[h->lognx].smem));
     if (h->rowv != v) {
         if (h->graph) cudaGraphExecDestroy(h->graph);
         if (h->graph_rows) cudaGraphExecDestroy(h->graph_rows);
@@ -781,7 +869,7 @@ static am_status time_steps(am_handle *h, int nsteps, cudaEvent_t e0, cudaEvent_
     return AM_OK;
 }
 
-am_status am_autotune(const am_params *p, int nsteps, double ms_col[3], double ms_row[2])
+am_status am_autotune(const am_params *p, int nsteps, double ms_col[3], double ms_row[3])
 {
     if (!p || nsteps < 1) return AM_ERR_ARG;
     am_handle *h = nullptr;

@@ -159,6 +159,7 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
     b->logny = ly;
     b->colv = col_variant(AM_FP32, ly);
     b->rowv = row_variant(AM_FP32, lx);
+    if (b->rowv == ROWV_TMA) b->rowv = 0;   // single-handle shape; its batched form is the lockstep pass
     b->loaded.assign(nmembers, 0);
     b->inside.assign(nmembers, 0);
     auto fail = [&](am_status s) {

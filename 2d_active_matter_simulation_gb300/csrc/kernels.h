@@ -45,8 +45,12 @@ inline int col_grid(const LaunchShape &s, int ntp, int W) { return (ntp * W + s.
 // Column-pass launch shapes: 0 wide, 1 narrow, 2 wide radix 8 (FP32 only).
 constexpr int NCOLV = 3;
 // Row-pass launch shapes: 0 radix 8 in lockstep (RowPass), 1 in sequence with
-// stashes (RowPassS; FP32 radix 16, double-float radix 8; Nx >= 512).
-constexpr int NROWV = 2;
+// stashes (RowPassS; FP32 radix 16, double-float radix 8; Nx >= 512), 2 the
+// lockstep pass with its input rows fetched by tensor-map copies (FP32,
+// Nx = 2048 and 4096; KernelTable::row_tma, used where a row's carried tiles
+// fit one exchange buffer, else shape 0 runs).
+constexpr int NROWV = 3;
+constexpr int ROWV_TMA = 2;
 constexpr int ROWS_LOG_MIN = 10;   // RowPassS needs Nx >= 512 (log2 9); it is built from 1024 up
 
 template <typename T>
@@ -59,6 +63,9 @@ struct KernelTable {
     LaunchShape rowfwd_shape[LOG_MAX + 1];
     void (*colfwd[LOG_MAX + 1])(const cpx<T> *, cpx<T> *, const cpx<T> *, int, int, int, int, int, int, int);
     LaunchShape colfwd_shape[LOG_MAX + 1];
+    void (*row_tma[LOG_MAX + 1])(StepArgs<T>, RowTma);   // [log2 Nx]; null: not built
+    LaunchShape row_tma_shape[LOG_MAX + 1];
+    int row_tma_cap[LOG_MAX + 1];                          // complex values one staging buffer holds
     void (*tile)(const cpx<T> *, cpx<T> *, int, int, int, int, int *);   // [ny][nxh] -> tiled
     void (*untile)(const cpx<T> *, cpx<T> *, int, int, int);  // tiled -> [ny][nxh]
     void (*lintab)(cpx<T> *, int, int, int, LinCoef);         // integrating-factor table

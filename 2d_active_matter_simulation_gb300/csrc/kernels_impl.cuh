@@ -17,6 +17,14 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
 }
 
 template <typename T, int LOG>
+__global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::MINB)
+    k_row_tma(StepArgs<T> a, const __grid_constant__ RowTma m)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); }, &m);
+}
+
+template <typename T, int LOG>
 __global__ void __launch_bounds__(RowPassS<T, LOG>::THREADS, RowPassS<T, LOG>::MINB) k_rows(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -116,6 +124,13 @@ struct Fill {
         t.row_shape[LOG][0] = {RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::smem_bytes(), RowKernel<T, LOG>::ROWS};
         // row shape 1, transforms in sequence: FP32 (radix 16) and
         // double-float (radix 8), Nx >= 1024
+        if constexpr (std::is_same_v<T, float> && RowKernel<T, LOG>::ROWS == 1 && !RowKernel<T, LOG>::SINGLE) {
+            // row shape 2: the lockstep pass with tensor-map row fetches
+            using RK = RowKernel<T, LOG>;
+            t.row_tma[LOG] = k_row_tma<T, LOG>;
+            t.row_tma_shape[LOG] = {RK::THREADS, RK::smem_bytes_tma(), RK::ROWS};
+            t.row_tma_cap[LOG] = RK::BUFS;
+        }
         if constexpr ((sizeof(T) == 4 || std::is_same_v<T, df>) && LOG >= ROWS_LOG_MIN) {
             t.row[LOG][1] = k_rows<T, LOG>;
             t.row_shape[LOG][1] = {RowPassS<T, LOG>::THREADS, RowPassS<T, LOG>::smem_bytes(), RowPassS<T, LOG>::ROWS};

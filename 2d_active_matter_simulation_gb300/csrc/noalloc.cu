@@ -181,7 +181,7 @@ am_status run(const am_params &p, void *w_hat, double *mean, int nsteps, double 
 
     const KernelTable<T> &K = table<T>();
     constexpr int prec = sizeof(T) == 8 ? AM_FP64 : AM_FP32;
-    const int rowv = row_variant(prec, lx2);
+    const int rowv = row_variant(prec, lx2) == ROWV_TMA ? 0 : row_variant(prec, lx2);   // no tensor maps here
     const LaunchShape &rs = K.row_shape[lx2][rowv];
     const int colv = col_variant(prec, ly2);
     const LaunchShape &cs = K.col_shape[ly2][colv];

@@ -326,6 +326,7 @@ am_status am_ragged_create(const am_params *params, const long long *nsteps, int
         r->cls[c].logny = keys[c].second;
         r->cls[c].colv = col_variant(AM_FP32, keys[c].second);
         r->cls[c].rowv = row_variant(AM_FP32, keys[c].first);
+        if (r->cls[c].rowv == ROWV_TMA) r->cls[c].rowv = 0;   // single-handle shape
     }
     size_t total = 0, stage = 0;
     for (int i = 0; i < nruns; i++) {

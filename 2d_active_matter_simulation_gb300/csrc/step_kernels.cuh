@@ -161,6 +161,58 @@ AF_HD void fft1(cpx<T> (&v)[FFT::R], int j, int c, const Buf &b, const cpx<T> *t
     else FFT::run(v, j, c, b, tw, tws, sync);
 }
 
+// Tensor-map (TMA) descriptors of the row pass's three input fields -- each an
+// opaque 128-byte CUtensorMap encoded on the host over the tiled layout as a
+// 3-D tensor {2 W floats (one 32-byte tile row), Ny rows, column tiles} --
+// and the split of a row's carried tiles into nbox boxes of `box` tiles
+// (a box dimension holds at most 256).
+struct alignas(128) TmaDesc {
+    unsigned char bytes[128];
+};
+struct RowTma {
+    TmaDesc map[3];   // fy, fx, fa: the order of the row pass's inputs
+    int nbox, box;
+};
+constexpr int TMA_WAIT_LIMIT = 1 << 20;   // mbarrier polls before a row gives up
+
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");   // visible to the copy engine
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+// One box of a 3-D tensor map into shared memory, completion counted on bar.
+__device__ __forceinline__ void tma_load_3d(void *dst, const TmaDesc *map, int c0, int c1, int c2,
+                                            unsigned long long *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_addr(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+        : "memory");
+}
+// Wait for phase `parity` of bar to complete, polling at most `limit` times.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, int limit)
+{
+    for (int it = 0; it < limit; it++) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+#endif
+
 // ------------------------------------------------------------------ row pass
 // One row y per group of TPC threads; a complex FFT of length M = Nx/2 per
 // real transform (the half-length real-FFT construction).  The Hermitian pairs
@@ -362,8 +414,20 @@ struct RowPass {
         return E + cmul(mk(D.y, -D.x), w);
     }
 
+    // With tma (FP32 rows of one CTA each, Nx >= 2048): the three input rows
+    // are fetched by tensor-map copies into the second set of exchange
+    // buffers (first written by the transforms' second exchange), issued by
+    // one thread and completed on an mbarrier at byte TMA_BAR, just past the
+    // buffers; the threads then read X(k), X(M-k) from shared memory instead
+    // of gathering one 8-byte value per 32-byte tile sector from global
+    // memory.  A wait that runs out sets Scalars::status (the host reports
+    // AM_ERR_TIMEOUT).
+    static constexpr size_t TMA_BAR = (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>);
+    static constexpr size_t smem_bytes_tma() { return TMA_BAR + 16; }
+
     template <class Sync>
-    static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync)
+    static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync,
+                           const RowTma *tma = nullptr)
     {
         const int rl = tid / TPC, j = tid % TPC;
         const int yy = bid * ROWS + rl;
@@ -379,11 +443,45 @@ struct RowPass {
         const cpx<T> wj = ldtw(a.twx, j);
         cpx<T> v[3][R];
         const cpx<T> *src[3] = {a.fy, a.fx, a.fa};
+        if (tma) {
+            static_assert(ROWS == 1 || sizeof(T) != 4 || LOGNX < 11, "tensor-map rows: one row per CTA");
+#ifdef __CUDA_ARCH__
+            if constexpr (sizeof(T) == 4 && ROWS == 1 && !SINGLE) {
+                unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + TMA_BAR);
+                if (tid == 0) mbar_init(bar, 1);
+                sync();
+                if (tid == 0) {
+                    mbar_expect_tx(bar, 3u * (unsigned)tma->nbox * (unsigned)tma->box * 32u);
+                    for (int f = 0; f < 3; f++)
+                        for (int c = 0; c < tma->nbox; c++)
+                            tma_load_3d(b1[f].d + (size_t)c * tma->box * Tile<T>::W, &tma->map[f], 0, y,
+                                        c * tma->box, bar);
+                }
+                if (!mbar_wait(bar, 0, TMA_WAIT_LIMIT)) {
+                    a.sc->status = 1;
+                    mbar_wait(bar, 0, TMA_WAIT_LIMIT);   // the copies still in flight
+                }
+            }
+#endif
 #pragma unroll
-        for (int f = 0; f < 3; f++) {
-            cpx<T> A[R], B[R];
-            load_pairs(A, B, src[f], j, y, ny, a.kxp);
-            pack_pairs(v[f], A, B, wj, j);
+            for (int f = 0; f < 3; f++) {
+                const cpx<T> *st = b1[f].d;   // the row, kx contiguous (tile by tile)
+                cpx<T> A[R], B[R];
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    const int k = j + r * TPC;
+                    A[r] = k <= a.kxp ? st[k] : mk<T>(0, 0);
+                    B[r] = M - k <= a.kxp ? st[M - k] : mk<T>(0, 0);
+                }
+                pack_pairs(v[f], A, B, wj, j);
+            }
+        } else {
+#pragma unroll
+            for (int f = 0; f < 3; f++) {
+                cpx<T> A[R], B[R];
+                load_pairs(A, B, src[f], j, y, ny, a.kxp);
+                pack_pairs(v[f], A, B, wj, j);
+            }
         }
         FFTi::template run_multi<3, SINGLE>(v, j, 0, b0, b1, a.twx, 2, sync);
 

@@ -312,13 +312,16 @@ long long am_footprint_bytes(const am_params *p);
  * (cuFFT picks its own plans, ActFlow_V3-2.cu:507-508). */
 am_status am_set_column_shape(int precision, int ny, int shape);
 int am_column_shape(int precision, int ny);   /* -1 for an unsupported size */
-/* The row pass has two launch shapes: 0 "lockstep" (radix-8 passes, 128
- * threads per 2048-point row, the three inverse transforms in lockstep) and 1
+/* The row pass has three launch shapes: 0 "lockstep" (radix-8 passes, 128
+ * threads per 2048-point row, the three inverse transforms in lockstep), 1
  * "sequence" (FP32 and double-float, Nx >= 1024: the transforms one after
  * another with two shared-memory stashes; FP32 with radix-16 passes, one
  * exchange fewer per transform and half the threads per row; double-float
  * with radix-8 passes and the transforms in a loop, a kernel small enough for
- * the instruction caches).  One choice per (precision, Nx), seeded with shape
+ * the instruction caches) and 2 "lockstep-tma" (FP32, Nx = 2048 and 4096:
+ * shape 0 with each CTA's three input rows fetched into shared memory by
+ * tensor-map copies; handles only, where the carried tiles of a row fit one
+ * exchange buffer -- otherwise it runs as shape 0).  One choice per (precision, Nx), seeded with shape
  * 0 (double-float from Nx = 1024: shape 1), used by every handle, batch and
  * ragged batch created afterwards; AM_ERR_UNSUPPORTED for a shape not built
  * for the precision and Nx.  No counterpart in the reference. */
@@ -329,8 +332,8 @@ int am_row_shape(int precision, int nx);      /* -1 for an unsupported size */
  * under each column-pass shape built for its precision, keep the fastest for
  * p's precision and Ny, then time each row-pass shape with that column shape
  * and keep the fastest for p's precision and Nx.  The times go to ms_col[3]
- * and ms_row[2] (either may be NULL; -1 for a shape not built). */
-am_status am_autotune(const am_params *p, int nsteps, double ms_col[3], double ms_row[2]);
+ * and ms_row[3] (either may be NULL; -1 for a shape not built). */
+am_status am_autotune(const am_params *p, int nsteps, double ms_col[3], double ms_row[3]);
 
 /* Number of kernel launches one step makes (for accounting). */
 int am_launches_per_step(const am_handle *h);

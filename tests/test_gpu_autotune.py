@@ -65,7 +65,7 @@ def test_autotune_row_shape_at_2048(am):
     oc, orr = am.column_shape("fp32", 256), am.row_shape("fp32", 2048)
     try:
         _, _, rtimes, rchosen = am.autotune(p, nsteps=5)
-        assert set(rtimes) == {"lockstep", "sequence"} and rchosen == min(rtimes, key=rtimes.get)
+        assert set(rtimes) == {"lockstep", "sequence", "lockstep-tma"} and rchosen == min(rtimes, key=rtimes.get)
     finally:
         am.set_column_shape("fp32", 256, oc)
         am.set_row_shape("fp32", 2048, orr)
@@ -139,3 +139,31 @@ def test_double_float_shapes(am):
         assert np.linalg.norm(res["sequence"] - res["lockstep"]) / np.linalg.norm(res["lockstep"]) < 1e-13
     finally:
         am.set_row_shape("df64", 2048, old)
+
+
+@pytest.mark.parametrize("nx,ny,kind", [(2048, 2048, "pruned"), (4096, 64, "pruned"), (2048, 128, "full")])
+def test_tensor_map_row_fetch_is_exact(am, nx, ny, kind):
+    """Row shape 2 fetches each CTA's input rows by tensor-map copies into
+    shared memory and reads them from there; the arithmetic is shape 0's, so
+    the steps are bit for bit shape 0's.  With full transforms at 2048 the
+    carried tiles do not fit one exchange buffer and shape 2 runs as shape 0."""
+    old = am.row_shape("fp32", nx)
+    w0 = am.ic_bandlimited(nx, ny, 9, 1.0, 8.0, 0.5)
+    if kind == "full":
+        w0[ny // 2, 3 * nx // 8] = 1e-3   # a mode outside the 1/2-rule ellipse: no pruning
+    res = {}
+    try:
+        for shape in ("lockstep", "lockstep-tma"):
+            am.set_row_shape("fp32", nx, shape)
+            sim = am.Solver(nx, ny, 2 * math.pi, 2 * math.pi * ny / nx, 1e-4, 3.5, -0.8, 0.01, gamma0=-0.045,
+                            gamma2=2.5e-5, dealias="half")
+            sim.set_state(w0.astype(np.complex64), (0.02 * nx * ny, -0.01 * nx * ny))
+            assert sim.kx_carried == (nx // 4 if kind == "pruned" else nx // 2)
+            e = sim.step(5)
+            w, m = sim.get_state()
+            sim.close()
+            res[shape] = (w, m, e)
+    finally:
+        am.set_row_shape("fp32", nx, old)
+    for a, b in zip(res["lockstep"], res["lockstep-tma"]):
+        assert np.array_equal(a, b)

@@ -492,7 +492,19 @@ def run_profile_case(args):
                     gamma0=PARAMS["gamma0"], gamma2=PARAMS["gamma2"], dealias=PARAMS["dealias"], precision=PRECISION)
     w0 = am.ic_bandlimited(NX, NY, SEED)
     sim.set_state(w0.astype(np.complex64) if PRECISION == "fp32" else w0, (0.0, 0.0))
-    e = sim.step(args.steps)
+    if args.profile_flush:
+        import torch
+        stream = torch.cuda.Stream()
+        sim.set_stream(stream.cuda_stream)
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                flush.zero_()
+                sim.step_async(1)
+        sim.sync()
+        e = np.zeros(0)
+    else:
+        e = sim.step(args.steps)
     sim.close()
     print(json.dumps({"profile_case": {"workload": WORKLOAD, "column_shape": col, "row_shape": row,
                                        "steps": args.steps, "energy_last": float(e[-1]) if len(e) else None}}),
@@ -885,6 +897,8 @@ def main():
     ap.add_argument("--profile-case", metavar="COL,ROW", default="",
                     help="configs 0/1: no timing; load the seeded field with the given column and row shapes "
                          "(e.g. wide8,lockstep) and run --steps steps: a short, deterministic command for ncu")
+    ap.add_argument("--profile-flush", action="store_true",
+                    help="with --profile-case: flush the L2 (256 MB write) before every step, as the timed region does")
     args = ap.parse_args()
     if args.impl == "ours":
         replica_setup()   # before torch or the solver touch a GPU

@@ -224,9 +224,32 @@ static EncodeTiled encode_tiled()
     return fn;
 }
 
+namespace af {
+// A tensor map of FP32 tiled fields for the row pass: {8 floats of a tile row,
+// Ny rows, nt column tiles, nfields fields field_stride bytes apart}, boxes of
+// one row and `box` tiles of one field.  False if the encoder is unavailable
+// or refuses the geometry.
+bool encode_row_map(TmaDesc *out, void *base, int ny, int nt, int nfields, size_t field_stride, int box)
+{
+    EncodeTiled enc = encode_tiled();
+    if (!enc) return false;
+    static_assert(sizeof(CUtensorMap) == sizeof(TmaDesc) && alignof(TmaDesc) >= alignof(CUtensorMap),
+                  "TmaDesc holds a CUtensorMap");
+    const int W = Tile<float>::W;
+    const cuuint64_t row_bytes = (cuuint64_t)(2 * W) * sizeof(float);
+    const cuuint64_t dims[4] = {(cuuint64_t)(2 * W), (cuuint64_t)ny, (cuuint64_t)nt, (cuuint64_t)nfields};
+    const cuuint64_t strides[3] = {row_bytes, row_bytes * ny, (cuuint64_t)field_stride};
+    const cuuint32_t boxd[4] = {(cuuint32_t)(2 * W), 1, (cuuint32_t)box, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    return enc(reinterpret_cast<CUtensorMap *>(out), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, boxd,
+               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace af
+
 // Tensor maps of the FP32 row pass's three inputs (fy, fx, fa) for the
 // handle's current pruning: each field as {8 floats of a tile row, Ny rows,
-// column tiles}, boxes of one row and `box` tiles, nbox boxes per row covering
+// column tiles, 1 field}, boxes of one row and `box` tiles, nbox boxes per row covering
 // the ntp carried tiles (a box may run past them: those tiles are read and
 // never used).  tma_ok only where those tiles fit one exchange
 // buffer of the row pass (else row shape 2 runs as shape 0).
@@ -242,24 +265,13 @@ static void prepare_row_tma(am_handle *h)
     // a 128-byte boundary of the staging buffer
     const int nbox = (a.ntp + 255) / 256, box = ((a.ntp + nbox - 1) / nbox + 3) / 4 * 4;
     if (nbox * box * W > K.row_tma_cap[h->lognx]) return;
-    EncodeTiled enc = encode_tiled();
-    if (!enc) return;
-    static_assert(sizeof(CUtensorMap) == sizeof(TmaDesc) && alignof(TmaDesc) >= alignof(CUtensorMap),
-                  "TmaDesc holds a CUtensorMap");
-    const cuuint64_t dims[3] = {(cuuint64_t)(2 * W), (cuuint64_t)h->p.ny, (cuuint64_t)h->nt};
-    const cuuint64_t strides[2] = {(cuuint64_t)(2 * W) * sizeof(float), (cuuint64_t)h->p.ny * 2 * W * sizeof(float)};
-    const cuuint32_t boxd[3] = {(cuuint32_t)(2 * W), 1, (cuuint32_t)box};
-    const cuuint32_t estr[3] = {1, 1, 1};
+    const size_t field_bytes = (size_t)2 * W * sizeof(float) * h->p.ny * h->nt;
     void *fields[3] = {h->fy, h->fx, h->fa};
-    for (int f = 0; f < 3; f++) {
-        CUresult r = enc(reinterpret_cast<CUtensorMap *>(&h->tma.map[f]), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
-                         fields[f], dims, strides, boxd, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS) return;
-    }
+    for (int f = 0; f < 3; f++)
+        if (!encode_row_map(&h->tma.map[f], fields[f], h->p.ny, h->nt, 1, field_bytes, box)) return;
     h->tma.nbox = nbox;
     h->tma.box = box;
+    h->tma.shared = 0;
     h->tma_ok = true;
 }
 

@@ -50,6 +50,10 @@ struct am_batch {
     int ntp_graph = -1;
     cudaGraphExec_t graph = nullptr;
     std::string err;
+    // lockstep row shape: its tensor-map form over one map of every member's
+    // fields, where the kernel is built and a row's carried tiles fit
+    RowTma tma{};
+    bool tma_ok = false;
 };
 
 #define BK(call)                                                  \
@@ -93,14 +97,38 @@ am_status build_graph(am_batch *b)
     }
     const KernelTable<float> &K = kernels_f32();
     const BatchTable &KB = kernels_batch_f32();
-    const LaunchShape &rs = K.row_shape[b->lognx][b->rowv];
+    // the lockstep row pass fetches its rows by tensor-map copies where the
+    // carried tiles fit one exchange buffer (results bit for bit the same)
+    b->tma_ok = false;
+    if (b->rowv == 0 && KB.row_tma[b->lognx]) {
+        const int W = Tile<float>::W;
+        const int nbox = (ntp + 255) / 256, box = ((ntp + nbox - 1) / nbox + 3) / 4 * 4;
+        if (nbox * box * W <= KB.row_tma_cap[b->lognx] &&
+            encode_row_map(&b->tma.map[0], b->fields, b->ny, b->nt, 7 * b->B, b->field_elems * sizeof(cpx<float>),
+                           box)) {
+            b->tma.nbox = nbox;
+            b->tma.box = box;
+            b->tma.shared = 1;
+            b->tma.slot[0] = 4;   // fy
+            b->tma.slot[1] = 3;   // fx
+            b->tma.slot[2] = 2;   // fa
+            b->tma_ok = true;
+        }
+    }
+    const LaunchShape &rs = b->tma_ok ? KB.row_tma_shape[b->lognx] : K.row_shape[b->lognx][b->rowv];
     const LaunchShape &cs = K.col_shape[b->logny][b->colv];
     const dim3 rgrid((b->ny + rs.per_block - 1) / rs.per_block, b->B);
     const dim3 cgrid(col_grid(cs, ntp, Tile<float>::W), b->B);
+    if (b->tma_ok && rs.smem > 48 * 1024)
+        BK(cudaFuncSetAttribute((const void *)KB.row_tma[b->lognx], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)rs.smem));
     cudaGraph_t g;
     BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 1; s <= 4; s++) {
-        KB.row[b->lognx][b->rowv]<<<rgrid, rs.threads, rs.smem, b->stream>>>(b->dargs);
+        if (b->tma_ok)
+            KB.row_tma[b->lognx]<<<rgrid, rs.threads, rs.smem, b->stream>>>(b->dargs, b->tma);
+        else
+            KB.row[b->lognx][b->rowv]<<<rgrid, rs.threads, rs.smem, b->stream>>>(b->dargs);
         KB.col[b->logny][b->colv][s]<<<cgrid, cs.threads, cs.smem, b->stream>>>(b->dargs);
     }
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
@@ -334,6 +362,11 @@ am_status am_batch_step(am_batch *b, int nsteps, double *energy, int *nan_member
                 b->err = "member " + std::to_string(m) + ": w(0,0) is NaN after step " +
                          std::to_string(done + sc[m].nan_step);
                 return AM_ERR_NAN;
+            }
+        for (int m = 0; m < b->B; m++)
+            if (sc[m].status != 0) {
+                b->err = "member " + std::to_string(m) + ": a row pass's tensor-map copies did not complete in time";
+                return AM_ERR_TIMEOUT;
             }
         done += k;
     }

@@ -109,6 +109,11 @@ constexpr int BATCH_LOG_MAX = 10;
 
 struct BatchTable {
     void (*row[LOG_MAX + 1][NROWV])(const StepArgs<float> *);       // [log2 Nx][shape]
+    // the lockstep row pass with tensor-map row fetches over one map of every
+    // member's fields (member m's field k is map field 7 m + k); null: not built
+    void (*row_tma[LOG_MAX + 1])(const StepArgs<float> *, RowTma);
+    LaunchShape row_tma_shape[LOG_MAX + 1];
+    int row_tma_cap[LOG_MAX + 1];   // complex values one staging buffer holds
     void (*col[LOG_MAX + 1][NCOLV][5])(const StepArgs<float> *);   // [log2 Ny][shape][mode]
 };
 
@@ -126,6 +131,11 @@ void set_row_variant(int prec, int lognx, int v);
 bool row_variant_built(int prec, int lognx, int v);
 
 const BatchTable &kernels_batch_f32();
+
+// A tensor map of FP32 tiled fields for the row pass's tensor-map fetch
+// (actflow_api.cu): {8 floats of a tile row, Ny rows, nt column tiles,
+// nfields fields field_stride bytes apart}, boxes of one row and `box` tiles.
+bool encode_row_map(TmaDesc *out, void *base, int ny, int nt, int nfields, size_t field_stride, int box);
 
 // Work-list kernels (kernels_queue.cu): one launch per pass over the runs of
 // several size classes.  Item = the run's argument index, the CTA index within

@@ -16,6 +16,15 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
 }
 
 template <typename T, int LOG>
+__global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::MINB)
+    k_row_b_tma(const StepArgs<T> *__restrict__ args, const __grid_constant__ RowTma m)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const StepArgs<T> a = args[blockIdx.y];
+    RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); }, &m, 7 * (int)blockIdx.y);
+}
+
+template <typename T, int LOG>
 __global__ void __launch_bounds__(RowPassS<T, LOG>::THREADS, RowPassS<T, LOG>::MINB)
     k_rows_b(const StepArgs<T> *__restrict__ args)
 {
@@ -38,6 +47,12 @@ struct FillB {
     static void run(BatchTable &t)
     {
         t.row[LOG][0] = k_row_b<float, LOG>;
+        if constexpr (!RowKernel<float, LOG>::SINGLE) {
+            using RK = RowKernel<float, LOG>;
+            t.row_tma[LOG] = k_row_b_tma<float, LOG>;
+            t.row_tma_shape[LOG] = {RK::THREADS, RK::smem_bytes_tma(), RK::ROWS};
+            t.row_tma_cap[LOG] = RK::BUFS;
+        }
         if constexpr (LOG >= ROWS_LOG_MIN) t.row[LOG][1] = k_rows_b<float, LOG>;
         t.col[LOG][0][0] = k_col_b<float, LOG, 0, 0>;
         t.col[LOG][0][1] = k_col_b<float, LOG, 1, 0>;

@@ -161,17 +161,21 @@ AF_HD void fft1(cpx<T> (&v)[FFT::R], int j, int c, const Buf &b, const cpx<T> *t
     else FFT::run(v, j, c, b, tw, tws, sync);
 }
 
-// Tensor-map (TMA) descriptors of the row pass's three input fields -- each an
-// opaque 128-byte CUtensorMap encoded on the host over the tiled layout as a
-// 3-D tensor {2 W floats (one 32-byte tile row), Ny rows, column tiles} --
-// and the split of a row's carried tiles into nbox boxes of `box` tiles
-// (a box dimension holds at most 256).
+// Tensor-map (TMA) descriptors of the row pass's three input fields -- opaque
+// 128-byte CUtensorMaps encoded on the host over the tiled layout as a 4-D
+// tensor {2 W floats (one 32-byte tile row), Ny rows, column tiles, fields} --
+// and the split of a row's carried tiles into nbox boxes of `box` tiles (a box
+// dimension holds at most 256).  A handle encodes one map per field (one
+// field each); an ensemble one map over all members' fields (field index =
+// member * 7 + slot[f]), with `shared` set.
 struct alignas(128) TmaDesc {
     unsigned char bytes[128];
 };
 struct RowTma {
     TmaDesc map[3];   // fy, fx, fa: the order of the row pass's inputs
     int nbox, box;
+    int shared;       // 1: map[0] covers every field, addressed by slot
+    int slot[3];      // field index of fy, fx, fa within a member's fields
 };
 constexpr int TMA_WAIT_LIMIT = 1 << 20;   // mbarrier polls before a row gives up
 
@@ -187,14 +191,14 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
 }
-// One box of a 3-D tensor map into shared memory, completion counted on bar.
-__device__ __forceinline__ void tma_load_3d(void *dst, const TmaDesc *map, int c0, int c1, int c2,
+// One box of a 4-D tensor map into shared memory, completion counted on bar.
+__device__ __forceinline__ void tma_load_4d(void *dst, const TmaDesc *map, int c0, int c1, int c2, int c3,
                                             unsigned long long *bar)
 {
     asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];\n" ::"r"(smem_addr(dst)),
-        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];\n" ::"r"(smem_addr(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
         : "memory");
 }
 // Wait for phase `parity` of bar to complete, polling at most `limit` times.
@@ -414,20 +418,21 @@ struct RowPass {
         return E + cmul(mk(D.y, -D.x), w);
     }
 
-    // With tma (FP32 rows of one CTA each, Nx >= 2048): the three input rows
-    // are fetched by tensor-map copies into the second set of exchange
-    // buffers (first written by the transforms' second exchange), issued by
-    // one thread and completed on an mbarrier at byte TMA_BAR, just past the
-    // buffers; the threads then read X(k), X(M-k) from shared memory instead
-    // of gathering one 8-byte value per 32-byte tile sector from global
-    // memory.  A wait that runs out sets Scalars::status (the host reports
-    // AM_ERR_TIMEOUT).
+    // With tma (FP32): each row's three input rows are fetched by tensor-map
+    // copies into that row's second set of exchange buffers (first written by
+    // the transforms' second exchange), issued by the row's thread j = 0 and
+    // completed on the row's mbarrier (ROWS of them at byte TMA_BAR, just past
+    // the buffers); the threads then read X(k), X(M-k) from shared memory
+    // instead of gathering one 8-byte value per 32-byte tile sector from
+    // global memory.  A wait that runs out sets Scalars::status (the host
+    // reports AM_ERR_TIMEOUT).  slot0: the member's first field index in an
+    // ensemble's shared map.
     static constexpr size_t TMA_BAR = (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>);
-    static constexpr size_t smem_bytes_tma() { return TMA_BAR + 16; }
+    static constexpr size_t smem_bytes_tma() { return TMA_BAR + ((size_t)8 * ROWS + 15) / 16 * 16; }
 
     template <class Sync>
     static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync,
-                           const RowTma *tma = nullptr)
+                           const RowTma *tma = nullptr, int slot0 = 0)
     {
         const int rl = tid / TPC, j = tid % TPC;
         const int yy = bid * ROWS + rl;
@@ -444,18 +449,19 @@ struct RowPass {
         cpx<T> v[3][R];
         const cpx<T> *src[3] = {a.fy, a.fx, a.fa};
         if (tma) {
-            static_assert(ROWS == 1 || sizeof(T) != 4 || LOGNX < 11, "tensor-map rows: one row per CTA");
 #ifdef __CUDA_ARCH__
-            if constexpr (sizeof(T) == 4 && ROWS == 1 && !SINGLE) {
-                unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + TMA_BAR);
-                if (tid == 0) mbar_init(bar, 1);
+            if constexpr (sizeof(T) == 4 && !SINGLE) {
+                unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + TMA_BAR) + rl;
+                if (j == 0) mbar_init(bar, 1);
                 sync();
-                if (tid == 0) {
+                if (j == 0) {
                     mbar_expect_tx(bar, 3u * (unsigned)tma->nbox * (unsigned)tma->box * 32u);
-                    for (int f = 0; f < 3; f++)
+                    for (int f = 0; f < 3; f++) {
+                        const TmaDesc *m = tma->shared ? &tma->map[0] : &tma->map[f];
+                        const int w = tma->shared ? slot0 + tma->slot[f] : 0;
                         for (int c = 0; c < tma->nbox; c++)
-                            tma_load_3d(b1[f].d + (size_t)c * tma->box * Tile<T>::W, &tma->map[f], 0, y,
-                                        c * tma->box, bar);
+                            tma_load_4d(b1[f].d + (size_t)c * tma->box * Tile<T>::W, m, 0, y, c * tma->box, w, bar);
+                    }
                 }
                 if (!mbar_wait(bar, 0, TMA_WAIT_LIMIT)) {
                     a.sc->status = 1;

@@ -228,6 +228,7 @@ am_status am_batch_create(const am_params *params, int nmembers, am_batch **out)
         cpx<float> *f = b->fields + (size_t)i * 7 * b->field_elems;
         a.u0 = f;
         a.acc = f + b->field_elems;
+        a.tma_field0 = 7 * i;   // fields [B][7] in one block: the ensemble's shared tensor map
         a.fa = f + 2 * b->field_elems;
         a.fx = f + 3 * b->field_elems;
         a.fy = f + 4 * b->field_elems;

@@ -110,7 +110,8 @@ constexpr int BATCH_LOG_MAX = 10;
 struct BatchTable {
     void (*row[LOG_MAX + 1][NROWV])(const StepArgs<float> *);       // [log2 Nx][shape]
     // the lockstep row pass with tensor-map row fetches over one map of every
-    // member's fields (member m's field k is map field 7 m + k); null: not built
+    // simulation's fields (simulation i's field k is map field
+    // args[i].tma_field0 + k); null: not built
     void (*row_tma[LOG_MAX + 1])(const StepArgs<float> *, RowTma);
     LaunchShape row_tma_shape[LOG_MAX + 1];
     int row_tma_cap[LOG_MAX + 1];   // complex values one staging buffer holds

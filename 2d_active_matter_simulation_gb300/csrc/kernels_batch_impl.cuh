@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>:
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const StepArgs<T> a = args[blockIdx.y];
-    RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); }, &m, 7 * (int)blockIdx.y);
+    RowKernel<T, LOG>::body(a, threadIdx.x, blockIdx.x, smem, []() { __syncthreads(); }, &m, a.tma_field0);
 }
 
 template <typename T, int LOG>

@@ -75,6 +75,8 @@ struct StepArgs {
     double mf_d2, mf_d6, mf_d6l, mf_d3l2;   // dt/2, dt/6, dt/6*lin_v, dt/3*lin2_v (dt as T, in double)
     double inv_2n3;                 // 1 / (2 N^3)
     int mode;                       // column pass: 0 = start from u0, 1..4 = RK stage
+    int tma_field0;                 // index of this simulation's u0 among the fields of a
+                                    // shared tensor map (ensemble members: 7 * member)
 };
 
 // Tile width in columns: 32 bytes of complex values.
@@ -425,8 +427,8 @@ struct RowPass {
     // the buffers); the threads then read X(k), X(M-k) from shared memory
     // instead of gathering one 8-byte value per 32-byte tile sector from
     // global memory.  A wait that runs out sets Scalars::status (the host
-    // reports AM_ERR_TIMEOUT).  slot0: the member's first field index in an
-    // ensemble's shared map.
+    // reports AM_ERR_TIMEOUT).  slot0: the simulation's first field index in
+    // a shared map (StepArgs::tma_field0).
     static constexpr size_t TMA_BAR = (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>);
     static constexpr size_t smem_bytes_tma() { return TMA_BAR + ((size_t)8 * ROWS + 15) / 16 * 16; }
 

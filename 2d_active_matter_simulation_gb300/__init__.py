@@ -478,7 +478,7 @@ def column_shape(precision, ny):
 # row-pass shapes: the three inverse transforms in lockstep (radix 8), or one
 # after another with shared-memory stashes ("sequence": FP32 radix 16,
 # double-float radix 8; Nx >= 1024), or lockstep with the input rows fetched
-# by tensor-map copies ("lockstep-tma": FP32, Nx = 2048 and 4096)
+# by tensor-map copies ("lockstep-tma": FP32, Nx >= 128)
 ROW_SHAPES = ("lockstep", "sequence", "lockstep-tma")
 
 

@@ -529,11 +529,12 @@ bool col_variant_built(int prec, int logny, int v)
 
 namespace {
 // [precision][log2 Nx]: 0 lockstep radix 8, 1 in sequence with stashes, 2
-// lockstep with tensor-map row fetches; seeded with 0, except FP32 at 2048 and
-// 4096 (shape 2: 12-15% faster row passes on GB300) and double-float from
-// Nx = 1024 (shape 1: the lockstep kernel outgrows the instruction caches)
+// lockstep with tensor-map row fetches; seeded with 0, except FP32 from 1024
+// (shape 2: 8-15% faster row passes on GB300 at 1024-4096; at 128-512 the
+// two are even or shape 0 ahead) and double-float from Nx = 1024 (shape 1:
+// the lockstep kernel outgrows the instruction caches)
 std::atomic<int> g_rowv[3][LOG_MAX + 1] = {
-    {{0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {2}, {2}},
+    {{0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {2}, {2}, {2}},
     {},
     {{0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {0}, {1}, {1}, {1}}};
 }  // namespace
@@ -541,10 +542,10 @@ std::atomic<int> g_rowv[3][LOG_MAX + 1] = {
 int row_variant(int prec, int lognx) { return g_rowv[pidx(prec)][lognx].load(std::memory_order_relaxed); }
 void set_row_variant(int prec, int lognx, int v) { g_rowv[pidx(prec)][lognx].store(v); }
 // In sequence with stashes: FP32 and double-float, Nx >= 1024.  Tensor-map
-// row fetches: FP32, Nx = 2048 and 4096 (one row per CTA).
+// row fetches: FP32, Nx >= 128.
 bool row_variant_built(int prec, int lognx, int v)
 {
-    if (v == ROWV_TMA) return prec == AM_FP32 && (lognx == 11 || lognx == 12);
+    if (v == ROWV_TMA) return prec == AM_FP32 && lognx >= 7 && lognx <= LOG_MAX;
     return v == 0 || (v == 1 && prec != AM_FP64 && lognx >= ROWS_LOG_MIN && lognx <= LOG_MAX);
 }
 

@@ -47,8 +47,8 @@ constexpr int NCOLV = 3;
 // Row-pass launch shapes: 0 radix 8 in lockstep (RowPass), 1 in sequence with
 // stashes (RowPassS; FP32 radix 16, double-float radix 8; Nx >= 512), 2 the
 // lockstep pass with its input rows fetched by tensor-map copies (FP32,
-// Nx = 2048 and 4096; KernelTable::row_tma, used where a row's carried tiles
-// fit one exchange buffer, else shape 0 runs).
+// Nx >= 128; KernelTable::row_tma, used where a row's carried tiles fit one
+// exchange buffer, else shape 0 runs).
 constexpr int NROWV = 3;
 constexpr int ROWV_TMA = 2;
 constexpr int ROWS_LOG_MIN = 10;   // RowPassS needs Nx >= 512 (log2 9); it is built from 1024 up

@@ -124,8 +124,7 @@ struct Fill {
         t.row_shape[LOG][0] = {RowKernel<T, LOG>::THREADS, RowKernel<T, LOG>::smem_bytes(), RowKernel<T, LOG>::ROWS};
         // row shape 1, transforms in sequence: FP32 (radix 16) and
         // double-float (radix 8), Nx >= 1024
-        if constexpr (std::is_same_v<T, float> && RowKernel<T, LOG>::ROWS == 1 && !RowKernel<T, LOG>::SINGLE &&
-                      LOG >= 11) {
+        if constexpr (std::is_same_v<T, float> && !RowKernel<T, LOG>::SINGLE && LOG >= 7) {
             // row shape 2: the lockstep pass with tensor-map row fetches
             using RK = RowKernel<T, LOG>;
             t.row_tma[LOG] = k_row_tma<T, LOG>;

@@ -318,11 +318,12 @@ int am_column_shape(int precision, int ny);   /* -1 for an unsupported size */
  * another with two shared-memory stashes; FP32 with radix-16 passes, one
  * exchange fewer per transform and half the threads per row; double-float
  * with radix-8 passes and the transforms in a loop, a kernel small enough for
- * the instruction caches) and 2 "lockstep-tma" (FP32, Nx = 2048 and 4096:
- * shape 0 with each CTA's three input rows fetched into shared memory by
- * tensor-map copies; handles only, where the carried tiles of a row fit one
- * exchange buffer -- otherwise it runs as shape 0).  One choice per (precision, Nx), seeded with shape
- * 0 (double-float from Nx = 1024: shape 1), used by every handle, batch and
+ * the instruction caches) and 2 "lockstep-tma" (FP32, Nx >= 128: shape 0
+ * with each row's three input rows fetched into shared memory by tensor-map
+ * copies, where the carried tiles of a row fit one exchange buffer --
+ * otherwise it runs as shape 0; ensembles use this fetch in their shape-0
+ * row pass).  One choice per (precision, Nx), seeded with shape 0 (FP32 from
+ * Nx = 1024: shape 2; double-float from Nx = 1024: shape 1), used by every handle, batch and
  * ragged batch created afterwards; AM_ERR_UNSUPPORTED for a shape not built
  * for the precision and Nx.  No counterpart in the reference. */
 am_status am_set_row_shape(int precision, int nx, int shape);

@@ -84,7 +84,8 @@ def test_autotune_keeps_the_faster_shape(am):
         times, chosen, rtimes, rchosen = am.autotune(p, nsteps=10)
         assert set(times) == {"wide", "narrow", "wide8"} and min(times.values()) > 0
         assert chosen == min(times, key=times.get)
-        assert set(rtimes) == {"lockstep"} and rchosen == "lockstep"   # the sequence shape is built from Nx = 1024
+        # the sequence shape is built from Nx = 1024
+        assert set(rtimes) == {"lockstep", "lockstep-tma"} and rchosen == min(rtimes, key=rtimes.get)
         # a batch created now uses the chosen shape and still matches a lone handle
         b = am.Batch([p, p])
         w0 = am.ic_bandlimited(512, 512, 5, rms=0.5).astype(np.complex64)
@@ -141,12 +142,14 @@ def test_double_float_shapes(am):
         am.set_row_shape("df64", 2048, old)
 
 
-@pytest.mark.parametrize("nx,ny,kind", [(2048, 2048, "pruned"), (4096, 64, "pruned"), (2048, 128, "full")])
+@pytest.mark.parametrize("nx,ny,kind", [(2048, 2048, "pruned"), (4096, 64, "pruned"), (2048, 128, "full"),
+                                        (1024, 256, "pruned"), (256, 512, "pruned"), (128, 64, "full")])
 def test_tensor_map_row_fetch_is_exact(am, nx, ny, kind):
-    """Row shape 2 fetches each CTA's input rows by tensor-map copies into
-    shared memory and reads them from there; the arithmetic is shape 0's, so
-    the steps are bit for bit shape 0's.  With full transforms at 2048 the
-    carried tiles do not fit one exchange buffer and shape 2 runs as shape 0."""
+    """Row shape 2 fetches each row's inputs by tensor-map copies into shared
+    memory and reads them from there (one row per CTA at 2048 and 4096,
+    several below); the arithmetic is shape 0's, so the steps are bit for bit
+    shape 0's.  With full transforms at 2048 the carried tiles do not fit one
+    exchange buffer and shape 2 runs as shape 0; at 128 they do."""
     old = am.row_shape("fp32", nx)
     w0 = am.ic_bandlimited(nx, ny, 9, 1.0, 8.0, 0.5)
     if kind == "full":

@@ -917,17 +917,24 @@ AF_HD void cp_async_wait_all()
 //    (ncu: 4x the L2 write sectors, 36 -> 47 us) than the extra CTAs won;
 //    below it the smaller CTAs win (ragged batch of 128^2..1024^2 grids
 //    +14%).
-//  * wide radix 8 (VAR 2, FP32 only): whole tiles as VAR 0, but radix-8
-//    passes with twice the threads per column (8 values each, up to 1024
-//    threads per CTA, 64 registers): one more exchange per transform, twice
-//    the warps per SM to hide the latency of a pass that is latency-bound
-//    with one 512-thread CTA per SM.
+//  * wide radix 8 (VAR 2, FP32 only): radix-8 passes with twice the threads
+//    per column (8 values each, 64 registers): one more exchange per
+//    transform, twice the warps per SM to hide the latency of a pass that is
+//    latency-bound with one 512-thread CTA per SM.  CTAs of at most 512
+//    threads, so at Ny = 2048 a CTA takes half a tile (two columns) and two
+//    independent CTAs share an SM, their load and transform phases
+//    interleaving (31.1 -> 29.3 us, though its stores cover half sectors);
+//    at 4096 a CTA takes half a tile with 1024 threads (512 would leave one
+//    column per CTA: 132 -> 153 us).
 // MODE 0 starts from u0 (after set_state), MODE 1..4 is the RK stage.
 // Launch: blockDim = THREADS, gridDim = ceil(columns carried / COLS).
 template <typename T, int LOGNY, int MODE, int VAR = (LOGNY < 11 ? 1 : 0)>
 struct ColPass {
     static constexpr bool NARROW = VAR == 1;
-    static constexpr int TMAX = VAR == 2 ? 1024 : 512;   // threads per CTA at most
+    // threads per CTA at most: 512, except the radix-8 shape at Ny = 4096
+    // (1024: a half tile per CTA; with 512 threads each CTA would take a
+    // single column and store quarter sectors)
+    static constexpr int TMAX = VAR == 2 && LOGNY >= 12 ? 1024 : 512;
     static constexpr int W = Tile<T>::W;
     static constexpr int LOGR = sizeof(T) == 4 && VAR != 2 ? 4 : 3;
     using FFTf = BlockFFT<T, LOGNY, LOGR, -1>;
@@ -941,7 +948,8 @@ struct ColPass {
     static constexpr int COLS = TILES * CW;                                // columns per CTA
     // CTAs per SM the registers allow (128 per thread at most; VAR 2: 64)
     static constexpr int MCAP = VAR == 2 ? 8 : 4;
-    static constexpr int MINB = THREADS >= TMAX ? 1 : (TMAX / THREADS > MCAP ? MCAP : TMAX / THREADS);
+    static constexpr int TREG = VAR == 2 ? 1024 : 512;   // threads per SM the registers are budgeted for
+    static constexpr int MINB = THREADS >= TREG ? 1 : (TREG / THREADS > MCAP ? MCAP : TREG / THREADS);
     // exchange slots: CW columns interleaved, idx + idx/8; one column: idx +
     // idx/16 (FP32) / idx + idx/8 (FP64), conflict-free for every pass of
     // these transforms (simulated bank pattern)

@@ -135,6 +135,7 @@ struct df2 {
 };
 __device__ __forceinline__ float2 f2_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ df2 df2_of(df a, df b) { return {make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)}; }
+__device__ __forceinline__ df2 df2_neg(df2 v) { return {make_float2(-v.hi.x, -v.hi.y), make_float2(-v.lo.x, -v.lo.y)}; }
 __device__ __forceinline__ df df2_first(df2 v) { return df(v.hi.x, v.lo.x); }
 __device__ __forceinline__ df df2_second(df2 v) { return df(v.hi.y, v.lo.y); }
 __device__ __forceinline__ df2 df2_fast_two_sum(float2 a, float2 b)

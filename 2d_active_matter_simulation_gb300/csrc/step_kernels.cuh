@@ -705,16 +705,43 @@ struct RowPassS {
         // stash slots): P to v, Q to s1
         T se = 0, sx = 0, sy = 0;
         const T lam = a.lam_s, bet = a.beta_s;
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+        if constexpr (std::is_same_v<T, df>) {
+            // double-float: the two points of a complex value as the two lanes
+            // of packed double-float operations (as the FP32 lockstep pass);
+            // the row sums accumulate per lane and meet at the end
+            const df2 zero = df2_of(df(0), df(0));
+            df2 se2 = zero, sx2 = zero, sy2 = zero;
+            const df2 lam2 = df2_of(lam, lam), bet2 = df2_of(bet, bet);
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const cpx<T> uyv = s1[j + r * TPC], uxv = s2[j + r * TPC], wv = v[r];
-            const T ux0 = uxv.x, uy0 = uyv.x, w0 = wv.x, ux1 = uxv.y, uy1 = uyv.y, w1 = wv.y;
-            const T q0 = ux0 * ux0 + uy0 * uy0, q1 = ux1 * ux1 + uy1 * uy1;
-            se += q0 + q1;
-            sx += q0 * ux0 + q1 * ux1;
-            sy += q0 * uy0 + q1 * uy1;
-            v[r] = mk(lam * w0 * ux0 + bet * q0 * uy0, lam * w1 * ux1 + bet * q1 * uy1);
-            s1[j + r * TPC] = mk(lam * w0 * uy0 - bet * q0 * ux0, lam * w1 * uy1 - bet * q1 * ux1);
+            for (int r = 0; r < R; r++) {
+                const cpx<T> uyv = s1[j + r * TPC], uxv = s2[j + r * TPC], wv = v[r];
+                const df2 ux = df2_of(uxv.x, uxv.y), uy = df2_of(uyv.x, uyv.y), w = df2_of(wv.x, wv.y);
+                const df2 q = df2_add(df2_mul(ux, ux), df2_mul(uy, uy));   // |u|^2
+                se2 = df2_add(se2, q);
+                sx2 = df2_add(sx2, df2_mul(q, ux));
+                sy2 = df2_add(sy2, df2_mul(q, uy));
+                const df2 lw = df2_mul(lam2, w), bq = df2_mul(bet2, q);
+                v[r] = df2_cpx(df2_add(df2_mul(lw, ux), df2_mul(bq, uy)));
+                s1[j + r * TPC] = df2_cpx(df2_add(df2_mul(lw, uy), df2_neg(df2_mul(bq, ux))));
+            }
+            se = df2_first(se2) + df2_second(se2);
+            sx = df2_first(sx2) + df2_second(sx2);
+            sy = df2_first(sy2) + df2_second(sy2);
+        } else
+#endif
+        {
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const cpx<T> uyv = s1[j + r * TPC], uxv = s2[j + r * TPC], wv = v[r];
+                const T ux0 = uxv.x, uy0 = uyv.x, w0 = wv.x, ux1 = uxv.y, uy1 = uyv.y, w1 = wv.y;
+                const T q0 = ux0 * ux0 + uy0 * uy0, q1 = ux1 * ux1 + uy1 * uy1;
+                se += q0 + q1;
+                sx += q0 * ux0 + q1 * ux1;
+                sy += q0 * uy0 + q1 * uy1;
+                v[r] = mk(lam * w0 * ux0 + bet * q0 * uy0, lam * w1 * ux1 + bet * q1 * uy1);
+                s1[j + r * TPC] = mk(lam * w0 * uy0 - bet * q0 * ux0, lam * w1 * uy1 - bet * q1 * ux1);
+            }
         }
         {
             T t0 = se, t1 = sx, t2 = sy;

@@ -334,6 +334,10 @@ bool harvest(Job &j)
         j.status = AM_ERR_NAN;
         j.err = "w(0,0) is NaN after step " + std::to_string(j.harvested + o.sc->nan_step);
     }
+    if (o.sc->status != 0 && j.status == AM_OK) {
+        j.status = AM_ERR_TIMEOUT;
+        j.err = "a row pass's tensor-map copies did not complete in time";
+    }
     j.harvested += o.k;
     o.busy = false;
     return true;

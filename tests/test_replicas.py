@@ -60,3 +60,18 @@ def test_two_gloo_ranks_take_the_max():
         p.join(timeout=60)
         assert p.exitcode == 0
     assert res == [(0, 11.0, (2, 0)), (1, 11.0, (2, 1))]
+
+
+def test_bench_reads_the_committed_traffic_captures():
+    """roofline.traffic comes from the committed ncu summaries: both passes'
+    per-launch DRAM bytes at 2048^2 and 4096^2, with the capture's build."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    for n in (2048, 4096):
+        bench.apply_preset(1, "fp32", n)
+        for key in ("row", "col"):
+            traffic, src = bench.ncu_traffic(key)
+            assert traffic and traffic > 1e6, (n, key)
+            assert src.startswith(f"profiles/ncu_traffic_{n}x{n}_fp32.txt (build ")

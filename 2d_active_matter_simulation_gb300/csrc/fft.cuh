@@ -138,6 +138,16 @@ template <>
 AF_HD cpx<df> scale(cpx<df> a, df s) { return df2_cpx(df2_mul(df2_of(a.x, a.y), df2_of(s, s))); }
 #endif
 
+// w + f n (double-float: as complex operations on the packed pipe).
+template <typename T>
+AF_HD cpx<T> axpy(cpx<T> w, T f, cpx<T> n)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    if constexpr (std::is_same_v<T, df>) return w + scale(n, f);
+#endif
+    return mk(w.x + f * n.x, w.y + f * n.y);
+}
+
 // Multiply by exp(SIGN * 2 pi i Q / R) for compile-time Q, R (R <= 32).
 // Multiples of pi/2 are exact sign swaps; the remaining angles are multiples
 // of pi/16, whose cosines are the constants below.

@@ -1096,10 +1096,15 @@ struct ColPass {
             for (int r = 0; r < R; r++) {
                 int iy = j + r * TPC;
                 T kyv = a.kyt[iy];
-                T tr = -kxv * ph[r].x - kyv * v[r].x;
-                T ti = -kxv * ph[r].y - kyv * v[r].y;
                 T m = (col && cm.keep(iy)) ? (T)1 : (T)0;
-                nl[r] = mk(-ti * m, tr * m);
+                if constexpr (std::is_same_v<T, df>) {   // complex operations, packed pipe
+                    const cpx<T> t = scale(ph[r], -kxv) + scale(v[r], -kyv);   // (tr, ti)
+                    nl[r] = scale(mk(-t.y, t.x), m);
+                } else {
+                    T tr = -kxv * ph[r].x - kyv * v[r].x;
+                    T ti = -kxv * ph[r].y - kyv * v[r].y;
+                    nl[r] = mk(-ti * m, tr * m);
+                }
             }
         }
 
@@ -1220,18 +1225,18 @@ struct ColPass {
                 }
                 if constexpr (MODE == 1) {
                     T f = dt / 6 * e1;
-                    w = mk(w.x + f * n.x, w.y + f * n.y);
-                    av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), e2);
+                    w = axpy(w, f, n);
+                    av[r] = scale(axpy(o, dt / 2, n), e2);
                 } else if constexpr (MODE == 2) {
                     T f = dt / 3 * e2;
-                    w = mk(w.x + f * n.x, w.y + f * n.y);
-                    av[r] = scale(mk(o.x + dt / 2 * n.x, o.y + dt / 2 * n.y), e2);
+                    w = axpy(w, f, n);
+                    av[r] = scale(axpy(o, dt / 2, n), e2);
                 } else if constexpr (MODE == 3) {
                     T f = dt / 3 * e2;
-                    w = mk(w.x + f * n.x, w.y + f * n.y);
-                    av[r] = scale(mk(o.x + dt * n.x, o.y + dt * n.y), e1);
+                    w = axpy(w, f, n);
+                    av[r] = scale(axpy(o, dt, n), e1);
                 } else {
-                    w = mk(w.x + dt / 6 * n.x, w.y + dt / 6 * n.y);
+                    w = axpy(w, dt / 6, n);
                     av[r] = w;   // next step: w_old = w_appr = w_new
                 }
                 if (active) {
@@ -1265,7 +1270,10 @@ struct ColPass {
                     const T kyv = a.kyt[iy];
                     const T k2 = kyv * kyv + kxv * kxv;
                     const T q = (f == 1 ? kyv : -kxv) / k2;
-                    v[r] = (col && (kx != 0 || iy != 0)) ? mk(-w.y * q, w.x * q) : mk<T>(0, 0);
+                    cpx<T> u;
+                    if constexpr (std::is_same_v<T, df>) u = scale(mk(-w.y, w.x), q);   // packed pipe
+                    else u = mk(-w.y * q, w.x * q);
+                    v[r] = (col && (kx != 0 || iy != 0)) ? u : mk<T>(0, 0);
                     if (owner && kx == 0 && iy == 0) v[r] = mk(f == 1 ? m0 : m1, (T)0);
                 }
             }

@@ -138,6 +138,19 @@ template <>
 AF_HD cpx<df> scale(cpx<df> a, df s) { return df2_cpx(df2_mul(df2_of(a.x, a.y), df2_of(s, s))); }
 #endif
 
+// a + s b, component by component (s = (sx, sy), used with s = +-1, where the
+// products are exact); FP32 on Blackwell: one packed fused multiply-add.
+template <typename T>
+AF_HD cpx<T> cfma(cpx<T> s, cpx<T> b, cpx<T> a) { return mk(a.x + s.x * b.x, a.y + s.y * b.y); }
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+template <>
+AF_HD cpx<float> cfma(cpx<float> s, cpx<float> b, cpx<float> a)
+{
+    const float2 r = __ffma2_rn(make_float2(s.x, s.y), make_float2(b.x, b.y), make_float2(a.x, a.y));
+    return mk(r.x, r.y);
+}
+#endif
+
 // w + f n (double-float: as complex operations on the packed pipe).
 template <typename T>
 AF_HD cpx<T> axpy(cpx<T> w, T f, cpx<T> n)
@@ -249,10 +262,12 @@ struct DFT {
 //   SWZ 1: idx ^ ((idx/16) % 16) row passes, FP32 (a permutation: no padding)
 //   SWZ 2: idx + idx/4          row passes, FP64
 //   SWZ 5: per exchange, keyed on the write stride NS of the exchange: NS = 2
-//          idx ^ ((idx/8) % 16), otherwise as SWZ 1 -- row passes, FP32:
-//          conflict-free for every exchange of the 1024-point transform
-//          (SWZ 1 alone: 1.25x the conflict-free wavefronts) and no worse at
-//          other lengths; put/get use the SWZ 1 map
+//          idx ^ ((idx/8) % 16), NS = 8 idx ^ (bit 6 of idx moved to bit 3),
+//          otherwise as SWZ 1 -- row passes, FP32: conflict-free for every
+//          exchange of the 1024-point transform (SWZ 1 alone: 1.25x the
+//          conflict-free wavefronts) and of the 512-point one (whose NS = 8
+//          writes were 2-way conflicts under SWZ 1), no worse at other
+//          lengths; put/get use the SWZ 1 map
 template <typename T, int W, int SWZ>
 struct XBuf {
     cpx<T> *d;
@@ -276,6 +291,9 @@ struct XBuf {
         if constexpr (SWZ == 5 && NSX == 2) {
             const int i = base + r * STRIDE;
             return (i ^ ((i >> 3) & 15)) * W + c;
+        } else if constexpr (SWZ == 5 && NSX == 8) {
+            const int i = base + r * STRIDE;
+            return (i ^ ((i >> 3) & 8)) * W + c;
         } else if constexpr (SWZ != 1 && SWZ != 5 && (STRIDE % (1 << SH)) == 0) {
             return (pad(base) + r * (STRIDE + (STRIDE >> SH))) * W + c;
         } else {

@@ -420,81 +420,13 @@ struct RowPass {
         return E + cmul(mk(D.y, -D.x), w);
     }
 
-    // With tma (FP32): each row's three input rows are fetched by tensor-map
-    // copies into that row's second set of exchange buffers (first written by
-    // the transforms' second exchange), issued by the row's thread j = 0 and
-    // completed on the row's mbarrier (ROWS of them at byte TMA_BAR, just past
-    // the buffers); the threads then read X(k), X(M-k) from shared memory
-    // instead of gathering one 8-byte value per 32-byte tile sector from
-    // global memory.  A wait that runs out sets Scalars::status (the host
-    // reports AM_ERR_TIMEOUT).  slot0: the simulation's first field index in
-    // a shared map (StepArgs::tma_field0).
-    static constexpr size_t TMA_BAR = (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>);
-    static constexpr size_t smem_bytes_tma() { return TMA_BAR + ((size_t)8 * ROWS + 15) / 16 * 16; }
-
+    // Real-space products over a thread's values (uy, ux, w in v[0..2]; each
+    // complex value carries two grid points): P replaces uy, Q replaces ux.
+    // Then the row sums of |u|^2, |u|^2 ux, |u|^2 uy, stored by thread j = 0.
     template <class Sync>
-    static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync,
-                           const RowTma *tma = nullptr, int slot0 = 0)
+    static AF_HD void products_and_sums(cpx<T> (&v)[3][R], const StepArgs<T> &a, int j, int y, bool active,
+                                        T *scratch, Sync &&sync)
     {
-        const int rl = tid / TPC, j = tid % TPC;
-        const int yy = bid * ROWS + rl;
-        const bool active = yy < a.ny;
-        const int y = active ? yy : a.ny - 1;   // inactive rows recompute the last row, never store
-        const int ny = a.ny;
-        cpx<T> *rbase = reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * NBUF * BUFS;
-        const Buf b0[3] = {Buf{rbase}, Buf{rbase + BUFS}, Buf{rbase + 2 * BUFS}};
-        const Buf b1[3] = {Buf{rbase + (3 - 3 * SINGLE) * BUFS}, Buf{rbase + (4 - 3 * SINGLE) * BUFS},
-                           Buf{rbase + (5 - 3 * SINGLE) * BUFS}};
-
-        // ---- C2R along x of uy, ux and w, the three transforms in lockstep
-        const cpx<T> wj = ldtw(a.twx, j);
-        cpx<T> v[3][R];
-        const cpx<T> *src[3] = {a.fy, a.fx, a.fa};
-        if (tma) {
-#ifdef __CUDA_ARCH__
-            if constexpr (sizeof(T) == 4 && !SINGLE) {
-                unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + TMA_BAR) + rl;
-                if (j == 0) mbar_init(bar, 1);
-                sync();
-                if (j == 0) {
-                    mbar_expect_tx(bar, 3u * (unsigned)tma->nbox * (unsigned)tma->box * 32u);
-                    for (int f = 0; f < 3; f++) {
-                        const TmaDesc *m = tma->shared ? &tma->map[0] : &tma->map[f];
-                        const int w = tma->shared ? slot0 + tma->slot[f] : 0;
-                        for (int c = 0; c < tma->nbox; c++)
-                            tma_load_4d(b1[f].d + (size_t)c * tma->box * Tile<T>::W, m, 0, y, c * tma->box, w, bar);
-                    }
-                }
-                if (!mbar_wait(bar, 0, TMA_WAIT_LIMIT)) {
-                    a.sc->status = 1;
-                    mbar_wait(bar, 0, TMA_WAIT_LIMIT);   // the copies still in flight
-                }
-            }
-#endif
-#pragma unroll
-            for (int f = 0; f < 3; f++) {
-                const cpx<T> *st = b1[f].d;   // the row, kx contiguous (tile by tile)
-                cpx<T> A[R], B[R];
-#pragma unroll
-                for (int r = 0; r < R; r++) {
-                    const int k = j + r * TPC;
-                    A[r] = k <= a.kxp ? st[k] : mk<T>(0, 0);
-                    B[r] = M - k <= a.kxp ? st[M - k] : mk<T>(0, 0);
-                }
-                pack_pairs(v[f], A, B, wj, j);
-            }
-        } else {
-#pragma unroll
-            for (int f = 0; f < 3; f++) {
-                cpx<T> A[R], B[R];
-                load_pairs(A, B, src[f], j, y, ny, a.kxp);
-                pack_pairs(v[f], A, B, wj, j);
-            }
-        }
-        FFTi::template run_multi<3, SINGLE>(v, j, 0, b0, b1, a.twx, 2, sync);
-
-        // ---- real-space products; v[f][r] holds x = 2n (real part) and
-        // 2n + 1 (imaginary part), n = j + r * TPC.  P replaces uy, Q replaces ux.
         T se = 0, sx = 0, sy = 0;
         const T lam = a.lam_s, bet = a.beta_s;
 #if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
@@ -535,17 +467,221 @@ struct RowPass {
                 v[1][r] = mk(lam * w0 * uy0 - bet * s0 * ux0, lam * w1 * uy1 - bet * s1 * ux1);
             }
         }
+        row_sum3(se, sx, sy, j, scratch, sync);
+        if (active && j == 0) {
+            a.rowp[y] = se;
+            a.rowp[a.ny + y] = sx;
+            a.rowp[2 * a.ny + y] = sy;
+        }
+    }
 
-        // ---- row sums of |u|^2, |u|^2 ux, |u|^2 uy over the row
-        {
-            T t0 = se, t1 = sx, t2 = sy;
-            row_sum3(t0, t1, t2, j, reinterpret_cast<T *>(b0[2].d), sync);
-            if (active && j == 0) {
-                a.rowp[y] = t0;
-                a.rowp[ny + y] = t1;
-                a.rowp[2 * ny + y] = t2;
+    // ---- Pruned transforms at Nx = 2048: four interleaved sub-sequences.
+    // With only kx <= K = Nx/4 carried (the 1/2 rule), a real row x(n) is
+    // band-limited, and each sub-sequence x_s(m) = x(4m + s), s = 0..3, is the
+    // real inverse transform of length K of
+    //   Y_s(c) = X(c) om^{cs} + conj(X(K - c) om^{(K - c)s}),  0 < c < K,
+    //   Y_s(0) = Re X(0) + 2 Re(X(K) i^s),                    om = exp(2 pi i / Nx)
+    // (frequency c collects kx = c and kx = c - K).  Pairing the real outputs,
+    //   z_0 = x_0 + i x_1 is the inverse transform of Z_0 = Y_0 + i Y_1,
+    //   z_1 = x_2 + i x_3 that of Z_1 = Y_2 + i Y_3,
+    // with Y_1 = om^c (X(c) - i conj X(K-c)), Y_2 = om^{2c} (X(c) - conj X(K-c)),
+    // Y_3 = om^{3c} (X(c) + i conj X(K-c)).  So a field takes two complex
+    // transforms of length K (half h = 0, 1 of the row's threads each) instead
+    // of one of length M = 2K.  Forward, with Z_h the transforms of the
+    // products' sub-sequence pairs (same layout), the carried outputs are
+    //   X(k) = sum_s om^{-ks} Y_s(k),  0 <= k < K,   X(K) = sum_s (-i)^s Y_s(0),
+    // with Y_{2h} = (Z_h(k) + conj Z_h(K-k)) / 2, Y_{2h+1} = (Z_h(k) - conj Z_h(K-k)) / 2i.
+    // At Nx = 2048 the 512-point transforms take two exchanges instead of the
+    // 1024-point transform's three.  Thread j = h TPQ + q holds c = q + r TPQ.
+    static constexpr int K = M / 2;
+    using FFTqi = BlockFFT<T, LOGM - 1, LOGR, +1>;
+    using FFTqf = BlockFFT<T, LOGM - 1, LOGR, -1>;
+    static constexpr int TPQ = FFTqi::TPC;
+    static constexpr int QS = Buf::slots(K);   // exchange slots of one half's transform
+    static constexpr bool QUARTER = sizeof(T) == 4 && !SINGLE && LOGNX == 11;
+
+    template <class Sync>
+    static AF_HD void quarter(const StepArgs<T> &a, int j, int y, bool active, const Buf (&b0)[3],
+                              const Buf (&b1)[3], bool staged, Sync &&sync)
+    {
+        static_assert(FFTqi::R == R && 2 * TPQ == TPC && FFTqf::NEXCH == 2 && TPQ % Tile<T>::W == 0 &&
+                          2 * QS <= BUFS && M <= BUFS,
+                      "two length-K transforms per row, radix R, two exchanges, both halves in one buffer");
+        constexpr int W = Tile<T>::W;
+        const int h = j / TPQ, q = j % TPQ;
+        const int ny = a.ny;
+        // ---- C2R of uy, ux, w: Z_h from x = X(c), xb = conj X(K - c),
+        // c = q + r TPQ, in one form for both halves (s = 1 - 2h):
+        //   Z_h = om^{2hc} (x + s xb) + i om^{(2h+1)c} (x - s i xb)
+        // (h = 0: Z_0 = Y_0 + i Y_1; h = 1: Z_1 = Y_2 + i Y_3).  The twiddles
+        // are table loads (the table holds om^{-m}), shared by the three fields.
+        cpx<T> v[3][R];
+        const cpx<T> *src[3] = {a.fy, a.fx, a.fa};
+        const size_t stride = (size_t)(TPQ / W) * ny * W;
+        const size_t ia = tidx<T>(q, y, ny), ib = tidx<T>(K - q, y, ny);
+        const T sg = h == 0 ? T(1) : T(-1);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int c = q + r * TPQ;
+            const cpx<T> ta = h ? ldtw(a.twx, 2 * c) : mk<T>(1, 0);
+            const cpx<T> tb = ldtw(a.twx, (2 * h + 1) * c);
+#pragma unroll
+            for (int f = 0; f < 3; f++) {
+                cpx<T> x, bq;
+                if (staged) {   // the row, kx contiguous, fetched by tensor-map copies
+                    x = c <= a.kxp ? b1[f].d[c] : mk<T>(0, 0);
+                    bq = K - c <= a.kxp ? b1[f].d[K - c] : mk<T>(0, 0);
+                } else {
+                    x = c <= a.kxp ? src[f][ia + r * stride] : mk<T>(0, 0);
+                    bq = K - c <= a.kxp ? src[f][ib - r * stride] : mk<T>(0, 0);
+                }
+                if (r == 0 && q == 0) {   // c = 0: Y_s(0) = Re X(0) + 2 Re(X(K) i^s)
+                    const T x0 = x.x, bx = bq.x + bq.x, by = bq.y + bq.y;
+                    v[f][0] = mk(x0 + sg * bx, x0 - sg * by);
+                } else {
+                    const cpx<T> xb = conj(bq);
+                    const cpx<T> E = cmulc(cfma(mk(sg, sg), xb, x), ta);
+                    const cpx<T> O = cmulc(cfma(mk(sg, -sg), mk(xb.y, xb.x), x), tb);
+                    v[f][r] = mk(E.x - O.y, E.y + O.x);
+                }
             }
         }
+        const Buf qb0[3] = {Buf{b0[0].d + h * QS}, Buf{b0[1].d + h * QS}, Buf{b0[2].d + h * QS}};
+        const Buf qb1[3] = {Buf{b1[0].d + h * QS}, Buf{b1[1].d + h * QS}, Buf{b1[2].d + h * QS}};
+        FFTqi::template run_multi<3, 0>(v, q, 0, qb0, qb1, a.twx, 4, sync);
+
+        // ---- products and row sums: z_h(m) = x(4m + 2h) + i x(4m + 2h + 1)
+        products_and_sums(v, a, j, y, active, reinterpret_cast<T *>(b0[2].d), sync);
+
+        // ---- R2C of P and Q; the pairing goes through b0, which the last
+        // pass (reading b1) left free
+        cpx<T>(&pq)[2][R] = *reinterpret_cast<cpx<T>(*)[2][R]>(&v[0]);
+        const Buf pb0[2] = {qb0[0], qb0[1]};
+        const Buf pb1[2] = {qb1[0], qb1[1]};
+        FFTqf::template run_multi<2, 0>(pq, q, 0, pb0, pb1, a.twx, 4, sync);
+#pragma unroll
+        for (int f = 0; f < 2; f++)
+#pragma unroll
+            for (int r = 0; r < R; r++) b0[f].d[h * K + q + r * TPQ] = pq[f][r];   // Z_h(c)
+        sync();
+        const int kend = a.ntp * W;   // the column pass reads kx < kend
+        // half h writes k = q + r TPQ for r in [h R/2, (h + 1) R/2), its own
+        // Z_h(k) from registers: with S_h = Z_h(k) + conj Z_h(K-k) and
+        // D_h = Z_h(k) - conj Z_h(K-k),
+        //   X(k) = (S_0 + om^{-k} D_0 / i + om^{-2k} S_1 + om^{-3k} D_1 / i) / 2,
+        //   X(K) = (S_0 - D_0 - S_1 + D_1) / 2  at k = 0
+#pragma unroll
+        for (int s = 0; s < R / 2; s++) {
+            const int k = q + (s + h * (R / 2)) * TPQ;
+            const int kr = (K - k) & (K - 1);
+            const cpx<T> t1 = ldtw(a.twx, k), t2 = ldtw(a.twx, 2 * k), t3 = ldtw(a.twx, 3 * k);
+#pragma unroll
+            for (int f = 0; f < 2; f++) {
+                const cpx<T> *z = b0[f].d;
+                const cpx<T> own = h ? pq[f][s + R / 2] : pq[f][s];
+                const cpx<T> oth = z[(1 - h) * K + k];
+                const cpx<T> z0 = h ? oth : own, z1 = h ? own : oth;
+                const cpx<T> z0r = conj(z[kr]), z1r = conj(z[K + kr]);
+                const cpx<T> S0 = z0 + z0r, D0 = z0 - z0r, S1 = z1 + z1r, D1 = z1 - z1r;
+                const cpx<T> X2 = S0 + cmul(mk(D0.y, -D0.x), t1) + cmul(S1, t2) + cmul(mk(D1.y, -D1.x), t3);
+                cpx<T> *dst = f == 0 ? a.P : a.Q;
+                if (active && k < kend) dst[tidx<T>(k, y, ny)] = scale(X2, (T)0.5);
+                if (s == 0 && active && j == 0 && K < kend)
+                    dst[tidx<T>(K, y, ny)] = scale(S0 - D0 - S1 + D1, (T)0.5);
+            }
+        }
+#pragma unroll
+        for (int f = 0; f < 2; f++) {
+            cpx<T> *dst = f == 0 ? a.P : a.Q;
+            for (int kx = K + 1 + j; active && kx < kend; kx += TPC) dst[tidx<T>(kx, y, ny)] = mk<T>(0, 0);
+        }
+    }
+
+    // With tma (FP32): each row's three input rows are fetched by tensor-map
+    // copies into that row's second set of exchange buffers (first written by
+    // the transforms' second exchange), issued by the row's thread j = 0 and
+    // completed on the row's mbarrier (ROWS of them at byte TMA_BAR, just past
+    // the buffers); the threads then read X(k), X(M-k) from shared memory
+    // instead of gathering one 8-byte value per 32-byte tile sector from
+    // global memory.  A wait that runs out sets Scalars::status (the host
+    // reports AM_ERR_TIMEOUT).  slot0: the simulation's first field index in
+    // a shared map (StepArgs::tma_field0).
+    static constexpr size_t TMA_BAR = (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>);
+    static constexpr size_t smem_bytes_tma() { return TMA_BAR + ((size_t)8 * ROWS + 15) / 16 * 16; }
+
+    template <class Sync>
+    static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync,
+                           const RowTma *tma = nullptr, int slot0 = 0)
+    {
+        const int rl = tid / TPC, j = tid % TPC;
+        const int yy = bid * ROWS + rl;
+        const bool active = yy < a.ny;
+        const int y = active ? yy : a.ny - 1;   // inactive rows recompute the last row, never store
+        const int ny = a.ny;
+        cpx<T> *rbase = reinterpret_cast<cpx<T> *>(smem) + (size_t)rl * NBUF * BUFS;
+        const Buf b0[3] = {Buf{rbase}, Buf{rbase + BUFS}, Buf{rbase + 2 * BUFS}};
+        const Buf b1[3] = {Buf{rbase + (3 - 3 * SINGLE) * BUFS}, Buf{rbase + (4 - 3 * SINGLE) * BUFS},
+                           Buf{rbase + (5 - 3 * SINGLE) * BUFS}};
+
+        const cpx<T> *src[3] = {a.fy, a.fx, a.fa};
+        if (tma) {
+#ifdef __CUDA_ARCH__
+            if constexpr (sizeof(T) == 4 && !SINGLE) {
+                unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem + TMA_BAR) + rl;
+                if (j == 0) mbar_init(bar, 1);
+                sync();
+                if (j == 0) {
+                    mbar_expect_tx(bar, 3u * (unsigned)tma->nbox * (unsigned)tma->box * 32u);
+                    for (int f = 0; f < 3; f++) {
+                        const TmaDesc *m = tma->shared ? &tma->map[0] : &tma->map[f];
+                        const int w = tma->shared ? slot0 + tma->slot[f] : 0;
+                        for (int c = 0; c < tma->nbox; c++)
+                            tma_load_4d(b1[f].d + (size_t)c * tma->box * Tile<T>::W, m, 0, y, c * tma->box, w, bar);
+                    }
+                }
+                if (!mbar_wait(bar, 0, TMA_WAIT_LIMIT)) {
+                    a.sc->status = 1;
+                    mbar_wait(bar, 0, TMA_WAIT_LIMIT);   // the copies still in flight
+                }
+            }
+#endif
+        }
+        if constexpr (QUARTER) {
+            if (a.kxp <= K) {
+                quarter(a, j, y, active, b0, b1, tma != nullptr, sync);
+                return;
+            }
+        }
+
+        // ---- C2R along x of uy, ux and w, the three transforms in lockstep
+        const cpx<T> wj = ldtw(a.twx, j);
+        cpx<T> v[3][R];
+        if (tma) {
+#pragma unroll
+            for (int f = 0; f < 3; f++) {
+                const cpx<T> *st = b1[f].d;   // the row, kx contiguous (tile by tile)
+                cpx<T> A[R], B[R];
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    const int k = j + r * TPC;
+                    A[r] = k <= a.kxp ? st[k] : mk<T>(0, 0);
+                    B[r] = M - k <= a.kxp ? st[M - k] : mk<T>(0, 0);
+                }
+                pack_pairs(v[f], A, B, wj, j);
+            }
+        } else {
+#pragma unroll
+            for (int f = 0; f < 3; f++) {
+                cpx<T> A[R], B[R];
+                load_pairs(A, B, src[f], j, y, ny, a.kxp);
+                pack_pairs(v[f], A, B, wj, j);
+            }
+        }
+        FFTi::template run_multi<3, SINGLE>(v, j, 0, b0, b1, a.twx, 2, sync);
+
+        // ---- real-space products (v[f][r] holds x = 2n in its real part and
+        // 2n + 1 in its imaginary part, n = j + r * TPC) and the row sums
+        products_and_sums(v, a, j, y, active, reinterpret_cast<T *>(b0[2].d), sync);
 
         // ---- R2C along x of P and Q in lockstep; the pairing exchange of each
         // uses the buffer its transform's last pass did not read

@@ -262,12 +262,13 @@ struct DFT {
 //   SWZ 1: idx ^ ((idx/16) % 16) row passes, FP32 (a permutation: no padding)
 //   SWZ 2: idx + idx/4          row passes, FP64
 //   SWZ 5: per exchange, keyed on the write stride NS of the exchange: NS = 2
-//          idx ^ ((idx/8) % 16), NS = 8 idx ^ (bit 6 of idx moved to bit 3),
-//          otherwise as SWZ 1 -- row passes, FP32: conflict-free for every
-//          exchange of the 1024-point transform (SWZ 1 alone: 1.25x the
-//          conflict-free wavefronts) and of the 512-point one (whose NS = 8
-//          writes were 2-way conflicts under SWZ 1), no worse at other
-//          lengths; put/get use the SWZ 1 map
+//          idx ^ ((idx/8) % 16), NS = 4 idx ^ (bits 5-6 of idx moved to bits
+//          2-3), NS = 8 idx ^ (bit 6 of idx moved to bit 3), otherwise as
+//          SWZ 1 -- row passes, FP32: conflict-free for every exchange of the
+//          transforms of 16 to 2048 points (SWZ 1 alone: 1.25x the
+//          conflict-free wavefronts at 1024 and 256 points, 1.17x at 2048;
+//          its NS = 4 and NS = 8 writes are 2-way conflicts); put/get use
+//          the SWZ 1 map
 template <typename T, int W, int SWZ>
 struct XBuf {
     cpx<T> *d;
@@ -291,6 +292,9 @@ struct XBuf {
         if constexpr (SWZ == 5 && NSX == 2) {
             const int i = base + r * STRIDE;
             return (i ^ ((i >> 3) & 15)) * W + c;
+        } else if constexpr (SWZ == 5 && NSX == 4) {
+            const int i = base + r * STRIDE;
+            return (i ^ ((i >> 3) & 12)) * W + c;
         } else if constexpr (SWZ == 5 && NSX == 8) {
             const int i = base + r * STRIDE;
             return (i ^ ((i >> 3) & 8)) * W + c;

@@ -513,8 +513,9 @@ struct RowPass {
         // ---- C2R of uy, ux, w: Z_h from x = X(c), xb = conj X(K - c),
         // c = q + r TPQ, in one form for both halves (s = 1 - 2h):
         //   Z_h = om^{2hc} (x + s xb) + i om^{(2h+1)c} (x - s i xb)
-        // (h = 0: Z_0 = Y_0 + i Y_1; h = 1: Z_1 = Y_2 + i Y_3).  The twiddles
-        // are table loads (the table holds om^{-m}), shared by the three fields.
+        // (h = 0: Z_0 = Y_0 + i Y_1; h = 1: Z_1 = Y_2 + i Y_3).  One twiddle
+        // per value from the table (which holds om^{-m}), its powers by
+        // products, shared by the three fields.
         cpx<T> v[3][R];
         const cpx<T> *src[3] = {a.fy, a.fx, a.fa};
         const size_t stride = (size_t)(TPQ / W) * ny * W;
@@ -523,8 +524,9 @@ struct RowPass {
 #pragma unroll
         for (int r = 0; r < R; r++) {
             const int c = q + r * TPQ;
-            const cpx<T> ta = h ? ldtw(a.twx, 2 * c) : mk<T>(1, 0);
-            const cpx<T> tb = ldtw(a.twx, (2 * h + 1) * c);
+            const cpx<T> t1 = ldtw(a.twx, c);                    // om^{-c}
+            const cpx<T> ta = h ? cmul(t1, t1) : mk<T>(1, 0);     // om^{-2hc}
+            const cpx<T> tb = h ? cmul(ta, t1) : t1;             // om^{-(2h+1)c}
 #pragma unroll
             for (int f = 0; f < 3; f++) {
                 cpx<T> x, bq;
@@ -574,7 +576,7 @@ struct RowPass {
         for (int s = 0; s < R / 2; s++) {
             const int k = q + (s + h * (R / 2)) * TPQ;
             const int kr = (K - k) & (K - 1);
-            const cpx<T> t1 = ldtw(a.twx, k), t2 = ldtw(a.twx, 2 * k), t3 = ldtw(a.twx, 3 * k);
+            const cpx<T> t1 = ldtw(a.twx, k), t2 = cmul(t1, t1), t3 = cmul(t2, t1);   // om^{-k}, om^{-2k}, om^{-3k}
 #pragma unroll
             for (int f = 0; f < 2; f++) {
                 const cpx<T> *z = b0[f].d;

@@ -498,7 +498,7 @@ struct RowPass {
     using FFTqf = BlockFFT<T, LOGM - 1, LOGR, -1>;
     static constexpr int TPQ = FFTqi::TPC;
     static constexpr int QS = Buf::slots(K);   // exchange slots of one half's transform
-    static constexpr bool QUARTER = sizeof(T) == 4 && !SINGLE && LOGNX == 11;
+    static constexpr bool QUARTER = !std::is_same_v<T, df> && !SINGLE && LOGNX == 11;   // FP32 and FP64
 
     template <class Sync>
     static AF_HD void quarter(const StepArgs<T> &a, int j, int y, bool active, const Buf (&b0)[3],

@@ -83,20 +83,23 @@ def test_fp32_integrating_factor_forms(am, orc, if_factors):
     assert rel(w, w64) < 2e-5
 
 
-def test_pruned_rows_match_full_transforms(am):
-    """FP32 at 2048^2: the pruned rows run as four interleaved sub-sequences
-    (two 512-point transforms per field), the full transforms as one
-    1024-point transform per field.  The same band-limited state through both
-    (the full path forced by one 1e-30 mode outside the 1/2-rule ellipse)
-    differs by the FP32 rounding of the nonlinear term alone, measured against
-    the nonlinear part of the step (the state minus a run without lambda and
-    beta): an error of 1e-5 in the nonlinear term would fail this."""
-    w0 = am.ic_bandlimited(N, N, seed=7, kmax=60.0, rms=2.0).astype(np.complex64)
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_pruned_rows_match_full_transforms(am, prec):
+    """At 2048^2 the pruned rows run as four interleaved sub-sequences (two
+    512-point transforms per field), the full transforms as one 1024-point
+    transform per field.  The same band-limited state through both (the full
+    path forced by one 1e-30 mode outside the 1/2-rule ellipse) differs by the
+    rounding of the nonlinear term alone, measured against the nonlinear part
+    of the step (the state minus a run without lambda and beta): an error of
+    1e-5 (FP32) or 1e-11 (FP64) in the nonlinear term would fail this."""
+    w0 = am.ic_bandlimited(N, N, seed=7, kmax=60.0, rms=2.0)
+    if prec == "fp32":
+        w0 = w0.astype(np.complex64)
     w0f = w0.copy()
     w0f[N // 2, 3 * N // 8] = 1e-30
 
     def run(w, lam, beta):
-        sim = am.Solver(N, N, L, L, DT, lam, ALPHA, beta, gamma0=G0, gamma2=G2, dealias="half")
+        sim = am.Solver(N, N, L, L, DT, lam, ALPHA, beta, gamma0=G0, gamma2=G2, dealias="half", precision=prec)
         sim.set_state(w)
         kc = sim.kx_carried
         sim.step(5)
@@ -110,4 +113,4 @@ def test_pruned_rows_match_full_transforms(am):
     assert kp == N // 4 and kf == N // 2
     nl = np.linalg.norm(wp - wl)
     assert nl > 1e-3 * np.linalg.norm(wp)   # the nonlinear term matters
-    assert np.linalg.norm(wp - wf) < 1e-5 * nl, np.linalg.norm(wp - wf) / nl
+    assert np.linalg.norm(wp - wf) < (1e-5 if prec == "fp32" else 1e-11) * nl, np.linalg.norm(wp - wf) / nl

@@ -148,20 +148,22 @@ def test_emulated_production_lengths(am, orc, emu, n, prec, kind):
 
 
 @pytest.mark.parametrize("n", [(2048, 16), (2048, 8), (512, 8)])
-def test_emulated_pruned_rows_match_full_transforms(am, orc, emu, n):
-    """FP32: one band-limited state through the pruned passes and through the
-    full transforms (forced by one 1e-30 mode outside the 1/2-rule ellipse).
-    At Nx = 2048 the pruned rows run as four interleaved sub-sequences (two
+@pytest.mark.parametrize("prec", [0, 1])
+def test_emulated_pruned_rows_match_full_transforms(am, orc, emu, n, prec):
+    """One band-limited state through the pruned passes and through the full
+    transforms (forced by one 1e-30 mode outside the 1/2-rule ellipse).  At
+    Nx = 2048 the pruned rows run as four interleaved sub-sequences (two
     512-point transforms per field) instead of one 1024-point transform, so
-    the two runs differ by the FP32 rounding of the nonlinear term alone (the
+    the two runs differ by the rounding of the nonlinear term alone (the
     linear part is computed the same way): measured about 1e-6 of the
-    nonlinear part of the step, where a 1e-4 change of lambda shows as 1e-4.
-    Nx = 512 has no such form and serves as the control."""
+    nonlinear part of the step in FP32 and 1e-15 in FP64, where a 1e-4 change
+    of lambda shows as 1e-4.  Nx = 512 has no such form and serves as the
+    control."""
     nx, ny = n
     w0 = np.fft.rfft2(np.random.default_rng(nx + 7 * ny).standard_normal((ny, nx))) * orc.mask(nx, ny, "half")
     w0f = w0.copy()
     w0f[ny // 2, 3 * nx // 8] = 1e-30
-    p = am.Params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, 0.0, 0.0, 0, am.DEALIAS["half"], 0)
+    p = am.Params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, 0.0, 0.0, 0, am.DEALIAS["half"], prec)
     wp, _, _ = _emu_run(am, emu, p, w0, (3.0, 1.0), 3)
     wf, _, _ = _emu_run(am, emu, p, w0f, (3.0, 1.0), 3)
     wo, _, _ = orc.run(orc.make_params(nx, ny, 10.0, 12.0, 1e-3, 7.0, -0.8, 0.01, dealias="half"), w0,
@@ -170,7 +172,7 @@ def test_emulated_pruned_rows_match_full_transforms(am, orc, emu, n):
                        (3.0, 1.0), 3, "f64")
     nl = np.linalg.norm(wo - wl)
     assert nl > 1e-4 * np.linalg.norm(wo)   # the nonlinear term matters
-    assert np.linalg.norm(wp - wf) < 1e-5 * nl
+    assert np.linalg.norm(wp - wf) < (1e-11 if prec else 1e-5) * nl
 
 
 @pytest.mark.parametrize("if_factors", ["float", "double"])

@@ -1027,6 +1027,25 @@ AF_HD void cp_async8(void *dst_smem, const void *src)
     for (int i = 0; i < 8; i++) static_cast<unsigned char *>(dst_smem)[i] = static_cast<const unsigned char *>(src)[i];
 #endif
 }
+// A load cached in L2 only: for values read once, so that they do not evict
+// the lines prefetched into L1 for later use.
+template <typename T>
+AF_HD cpx<T> ld_stream(const cpx<T> *p)
+{
+#ifdef __CUDA_ARCH__
+    cpx<T> r;
+    if constexpr (sizeof(cpx<T>) == 8) {
+        const float2 v = __ldcg(reinterpret_cast<const float2 *>(p));
+        memcpy(&r, &v, sizeof r);
+    } else {
+        const float4 v = __ldcg(reinterpret_cast<const float4 *>(p));
+        memcpy(&r, &v, sizeof r);
+    }
+    return r;
+#else
+    return *p;
+#endif
+}
 // Hint to bring the line holding p into this SM's L1 (no register, no wait).
 AF_HD void prefetch_l1(const void *p)
 {
@@ -1135,9 +1154,16 @@ struct ColPass {
     static constexpr size_t LIM = (size_t)228 * 1024 / MINB - 1024 < (size_t)227 * 1024
                                       ? (size_t)228 * 1024 / MINB - 1024
                                       : (size_t)227 * 1024;
-    static constexpr bool PS = XB + SCB + WPB <= LIM;                     // Scalars
-    static constexpr bool PF = PS && XB + SCB + PFB + WPB <= LIM;         // + row sums
-    static constexpr bool PM = PF && XB + SCB + PFB + MIB + WPB <= LIM;   // + mirror column
+    // The radix-8 shape at Ny >= 4096 stages only the Scalars: its owner
+    // prefetches the row sums and the mirror column into L1 instead, because
+    // every CTA of the launch would reserve those buffers, and the
+    // shared-memory carve-out they take comes out of the L1 that holds the
+    // stage inputs prefetched during Q's transform (4096^2: 156 -> 75 KB per
+    // CTA, column pass 131 -> 122 us; at 2048 the change measured neutral).
+    static constexpr bool OWN = !(VAR == 2 && LOGNY >= 12);
+    static constexpr bool PS = XB + SCB + WPB <= LIM;                            // Scalars
+    static constexpr bool PF = OWN && PS && XB + SCB + PFB + WPB <= LIM;         // + row sums
+    static constexpr bool PM = PF && XB + SCB + PFB + MIB + WPB <= LIM;          // + mirror column
     static constexpr size_t O_SC = XB, O_PF = O_SC + SCB, O_MI = O_PF + (PF ? PFB : 0);
     static constexpr size_t O_WP = O_MI + (PM ? MIB : 0);
     static constexpr int CE = 16 / (int)sizeof(T);                     // row sums per 16-byte copy
@@ -1194,6 +1220,18 @@ struct ColPass {
                             cp_async16(rsm + (size_t)k * ny + q * CE, a.rowp + (size_t)k * ny + q * CE);
                 }
                 cp_async_commit();
+                if constexpr (!PF) {   // the row sums, 128-byte lines
+                    constexpr int PL = 128 / (int)sizeof(T);
+                    for (int q = tid; q < 3 * ny / PL; q += THREADS) prefetch_l1(a.rowp + (size_t)q * PL);
+                }
+                if constexpr (!PM) {   // the mirror source: four tile rows per line (MODE 1), or hin
+                    if constexpr (MODE == 1) {
+                        for (int q = tid; q < ny / 4; q += THREADS) prefetch_l1(a.u0 + (size_t)(4 * q) * W);
+                    } else {
+                        constexpr int HL = 128 / (int)sizeof(cpx<T>);
+                        for (int q = tid; q < ny / HL; q += THREADS) prefetch_l1(hin + (size_t)q * HL);
+                    }
+                }
             }
         }
 
@@ -1202,12 +1240,12 @@ struct ColPass {
         if constexpr (MODE != 0) {
             cpx<T> ph[R], v[R];
 #pragma unroll
-            for (int r = 0; r < R; r++) v[r] = active ? a.P[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
+            for (int r = 0; r < R; r++) v[r] = active ? ld_stream(a.P + cbase + (size_t)(j + r * TPC) * W) : mk<T>(0, 0);
             fft1<FFTf>(v, j, c, buf, a.twy, 1, sync);
 #pragma unroll
             for (int r = 0; r < R; r++) ph[r] = v[r];
 #pragma unroll
-            for (int r = 0; r < R; r++) v[r] = active ? a.Q[cbase + (size_t)(j + r * TPC) * W] : mk<T>(0, 0);
+            for (int r = 0; r < R; r++) v[r] = active ? ld_stream(a.Q + cbase + (size_t)(j + r * TPC) * W) : mk<T>(0, 0);
             // the stage's inputs move towards L1 while Q is transformed
             if (active) {
 #pragma unroll

@@ -39,8 +39,9 @@ AF_HD cpx<T> lintab_value(const LinCoef &c, int ny, int kx, int y)
     return mk((T)exp(L * c.dt / 2), (T)exp(L * c.dt));
 }
 
-// CTAs of a step column-pass launch over ntp column tiles of W columns.
-inline int col_grid(const LaunchShape &s, int ntp, int W) { return (ntp * W + s.per_block - 1) / s.per_block; }
+// CTAs of a step column-pass launch over ntp column tiles of W columns: the
+// column groups, then one reducer CTA (ColPass::reduce_scalars).
+inline int col_grid(const LaunchShape &s, int ntp, int W) { return (ntp * W + s.per_block - 1) / s.per_block + 1; }
 
 // Column-pass launch shapes: 0 wide, 1 narrow, 2 wide radix 8 (FP32 only).
 constexpr int NCOLV = 3;

@@ -5,16 +5,17 @@
 // (nonl_func ActFlow_V3-2.cu:1036-1088, integrate_func_* 940-1018,
 // reality_func 1228-1243).  Here a stage is two kernels:
 //
-//   row pass  (one CTA row group per y):   C2R along x of a, ux, uy ->
-//             real-space products P = lam' w ux + beta' |u|^2 uy,
-//             Q = lam' w uy - beta' |u|^2 ux and the per-row sums of |u|^2
-//             (energy) and |u|^2 u (mean-flow right-hand side) -> R2C along x
-//             of P and Q.
-//   column pass (one CTA per tile of kx columns): forward FFT along y of P, Q
-//             -> N = i (-kx P^ - ky Q^) * mask -> Hermitian repair of the
-//             kx = 0 column of the accumulator -> RK stage combination with the
-//             integrating factors -> mean-flow scalar update -> Biot-Savart ->
-//             inverse FFT along y of the next stage input a, ux, uy.
+//   row pass  (one CTA row group per y):   C2R along x of a, ux, uy (the
+//             mean velocity added as their k = 0 mode) -> real-space products
+//             P = lam' w ux + beta' |u|^2 uy, Q = lam' w uy - beta' |u|^2 ux
+//             and the per-row sums of |u|^2 (energy) and |u|^2 u (mean-flow
+//             right-hand side) -> R2C along x of P and Q.
+//   column pass (one CTA per group of kx columns, plus one reducer CTA):
+//             forward FFT along y of P, Q -> N = i (-kx P^ - ky Q^) * mask ->
+//             Hermitian repair of the kx = 0 column of the accumulator -> RK
+//             stage combination with the integrating factors -> Biot-Savart ->
+//             inverse FFT along y of the next stage input a, ux, uy; the
+//             reducer CTA sums the row sums and updates the mean-flow scalars.
 //
 // By linearity F[lam' w ux] + F[beta' |u|^2 uy] = F[P], so the reference's four
 // forward transforms of separate products (ActFlow_V3-2.cu:1069-1072) collapse
@@ -219,6 +220,18 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 }
 #endif
 
+// The mean velocity, component d (the scaled mean Nx Ny <u> of the stage
+// input, Scalars::m_appr, set by the column pass before).  It is the k = 0
+// mode of ux and uy (nonl_subfunc_0, ActFlow_V3-2.cu:1053-1054); the row
+// passes add it to Re X(kx = 0) of each row before the C2R along x, which
+// adds it to every real-space value, as the unnormalised inverse transforms
+// of that mode do.
+template <typename T>
+AF_HD T mean_velocity(const StepArgs<T> &a, int d)
+{
+    return (T)a.sc->m_appr[d];
+}
+
 // ------------------------------------------------------------------ row pass
 // One row y per group of TPC threads; a complex FFT of length M = Nx/2 per
 // real transform (the half-length real-FFT construction).  The Hermitian pairs
@@ -311,7 +324,8 @@ struct RowPass {
     // The pre/post-processing twiddle W^k = exp(-2 pi i k / Nx) for
     // k = j + r TPC equals W^j * exp(-2 pi i r / (2R)) (Nx = 2 R TPC): one table
     // value per thread (wj) times a compile-time rotation.
-    static AF_HD void pack_pairs(cpx<T> (&v)[R], const cpx<T> (&A)[R], const cpx<T> (&B)[R], cpx<T> wj, int j)
+    static AF_HD void pack_pairs(cpx<T> (&v)[R], const cpx<T> (&A)[R], const cpx<T> (&B)[R], cpx<T> wj, int j,
+                                 T m)
     {
         static_for<0, R>([&](auto rc) {
             constexpr int r = decltype(rc)::value;
@@ -319,6 +333,7 @@ struct RowPass {
             if (r == 0 && j == 0) {   // X(0), X(M): imaginary parts dropped, as a half-plane C2R does
                 a.y = 0;
                 b.y = 0;
+                a.x = a.x + m;        // the field's mean (the k = 0 mode), see mean_velocity
             }
             const cpx<T> E = a + b;
             const cpx<T> O = rot<r, 2 * R, +1>(cmulc(a - b, wj));   // (A - conj B) conj(W^k)
@@ -502,7 +517,7 @@ struct RowPass {
 
     template <class Sync>
     static AF_HD void quarter(const StepArgs<T> &a, int j, int y, bool active, const Buf (&b0)[3],
-                              const Buf (&b1)[3], bool staged, Sync &&sync)
+                              const Buf (&b1)[3], bool staged, Sync &&sync, T mx, T my)
     {
         static_assert(FFTqi::R == R && 2 * TPQ == TPC && FFTqf::NEXCH == 2 && TPQ % Tile<T>::W == 0 &&
                           2 * QS <= BUFS && M <= BUFS,
@@ -537,8 +552,8 @@ struct RowPass {
                     x = c <= a.kxp ? src[f][ia + r * stride] : mk<T>(0, 0);
                     bq = K - c <= a.kxp ? src[f][ib - r * stride] : mk<T>(0, 0);
                 }
-                if (r == 0 && q == 0) {   // c = 0: Y_s(0) = Re X(0) + 2 Re(X(K) i^s)
-                    const T x0 = x.x, bx = bq.x + bq.x, by = bq.y + bq.y;
+                if (r == 0 && q == 0) {   // c = 0: Y_s(0) = Re X(0) + 2 Re(X(K) i^s), Re X(0) with the mean
+                    const T x0 = x.x + (f == 0 ? my : f == 1 ? mx : T(0)), bx = bq.x + bq.x, by = bq.y + bq.y;
                     v[f][0] = mk(x0 + sg * bx, x0 - sg * by);
                 } else {
                     const cpx<T> xb = conj(bq);
@@ -624,6 +639,8 @@ struct RowPass {
         const Buf b0[3] = {Buf{rbase}, Buf{rbase + BUFS}, Buf{rbase + 2 * BUFS}};
         const Buf b1[3] = {Buf{rbase + (3 - 3 * SINGLE) * BUFS}, Buf{rbase + (4 - 3 * SINGLE) * BUFS},
                            Buf{rbase + (5 - 3 * SINGLE) * BUFS}};
+        // the mean velocity, added to Re X(0) of ux and uy before the C2R
+        const T mx = mean_velocity(a, 0), my = mean_velocity(a, 1);
 
         const cpx<T> *src[3] = {a.fy, a.fx, a.fa};
         if (tma) {
@@ -650,7 +667,7 @@ struct RowPass {
         }
         if constexpr (QUARTER) {
             if (a.kxp <= K) {
-                quarter(a, j, y, active, b0, b1, tma != nullptr, sync);
+                quarter(a, j, y, active, b0, b1, tma != nullptr, sync, mx, my);
                 return;
             }
         }
@@ -669,14 +686,14 @@ struct RowPass {
                     A[r] = k <= a.kxp ? st[k] : mk<T>(0, 0);
                     B[r] = M - k <= a.kxp ? st[M - k] : mk<T>(0, 0);
                 }
-                pack_pairs(v[f], A, B, wj, j);
+                pack_pairs(v[f], A, B, wj, j, f == 0 ? my : f == 1 ? mx : T(0));
             }
         } else {
 #pragma unroll
             for (int f = 0; f < 3; f++) {
                 cpx<T> A[R], B[R];
                 load_pairs(A, B, src[f], j, y, ny, a.kxp);
-                pack_pairs(v[f], A, B, wj, j);
+                pack_pairs(v[f], A, B, wj, j, f == 0 ? my : f == 1 ? mx : T(0));
             }
         }
         FFTi::template run_multi<3, SINGLE>(v, j, 0, b0, b1, a.twx, 2, sync);
@@ -764,7 +781,7 @@ struct RowPassS {
 
     // X(k), X(M-k) for k = j + r TPC packed into Z(k) (as RowPass::pack_pairs;
     // the twiddle of k is wj times a compile-time rotation by r / (2R) turns).
-    static AF_HD void load_pack(cpx<T> (&v)[R], const cpx<T> *src, int j, int y, int ny, int kxp, cpx<T> wj)
+    static AF_HD void load_pack(cpx<T> (&v)[R], const cpx<T> *src, int j, int y, int ny, int kxp, cpx<T> wj, T m)
     {
         constexpr int W = Tile<T>::W;
         const cpx<T> *pa = src + tidx<T>(j, y, ny);
@@ -779,6 +796,7 @@ struct RowPassS {
             if (r == 0 && j == 0) {   // X(0), X(M): imaginary parts dropped, as a half-plane C2R does
                 a.y = 0;
                 b.y = 0;
+                a.x = a.x + m;        // the field's mean (the k = 0 mode), see mean_velocity
             }
             const cpx<T> Ev = a + b;
             const cpx<T> O = rot<r, 2 * R, +1>(cmulc(a - b, wj));
@@ -825,12 +843,13 @@ struct RowPassS {
         cpx<T> *s2 = s1 + M;        // ux, then P^ for its pairing
         T *scr = reinterpret_cast<T *>(reinterpret_cast<cpx<T> *>(smem) + (size_t)ROWS * SLOTS) + rl * 3 * 32;
         const cpx<T> wj = ldtw(a.twx, j);
+        const T mx = mean_velocity(a, 0), my = mean_velocity(a, 1);   // added to Re X(0) of ux, uy
 
         // ---- C2R along x of uy and ux (stashed), then w (kept in registers)
         cpx<T> v[R];
 #pragma unroll(F32 ? 3 : 1)
         for (int f = 0; f < 3; f++) {
-            load_pack(v, f == 0 ? a.fy : f == 1 ? a.fx : a.fa, j, y, ny, a.kxp, wj);
+            load_pack(v, f == 0 ? a.fy : f == 1 ? a.fx : a.fa, j, y, ny, a.kxp, wj, f == 0 ? my : f == 1 ? mx : T(0));
             fft1<FFTi>(v, j, 0, xb, a.twx, 2, sync);
             if (f < 2) {
                 cpx<T> *st = f == 0 ? s1 : s2;
@@ -1140,39 +1159,111 @@ struct ColPass {
     using Buf = XBuf<T, CW, (CW == 1 && sizeof(T) == 4) ? 3 : 0>;
     static constexpr int BUFS = (Buf::slots(L) + 7) / 8 * 8;
     // Shared memory, within MINB CTAs per SM: the exchange buffers; then what
-    // CTA 0 fetches at kernel start in stages 1-4 so that its extra serial
-    // work (the mean flow, the energy, the Hermitian repair) runs from shared
-    // memory: the Scalars, the row sums, the source of the kx = 0 column's
-    // mirror values (in that order of priority, each where it fits); then one
-    // partial sum per warp.
+    // CTA 0 (holding column kx = 0) fetches at kernel start in stages 1-4 so
+    // that its extra work (the Hermitian repair, the step counters) runs from
+    // shared memory: the Scalars, then the source of the kx = 0 column's
+    // mirror values (each where it fits); then one partial sum per warp (the
+    // reducer CTA's row-sum reduction).
     static constexpr size_t XB = (size_t)TILES * BUFS * sizeof(cpx<T>);
     static constexpr size_t SCB = sizeof(Scalars);
     static constexpr size_t MIB = (size_t)L * sizeof(cpx<T>);
-    static constexpr size_t PFB = (size_t)3 * L * sizeof(T);
     static constexpr int NW = THREADS / 32 > 0 ? THREADS / 32 : 1;
     static constexpr size_t WPB = (size_t)3 * NW * sizeof(RowAcc<T>);
     static constexpr size_t LIM = (size_t)228 * 1024 / MINB - 1024 < (size_t)227 * 1024
                                       ? (size_t)228 * 1024 / MINB - 1024
                                       : (size_t)227 * 1024;
-    // The radix-8 shape at Ny >= 4096 stages only the Scalars: its owner
-    // prefetches the row sums and the mirror column into L1 instead, because
-    // every CTA of the launch would reserve those buffers, and the
-    // shared-memory carve-out they take comes out of the L1 that holds the
-    // stage inputs prefetched during Q's transform (4096^2: 156 -> 75 KB per
-    // CTA, column pass 131 -> 122 us; at 2048 the change measured neutral).
+    // The radix-8 shape at Ny >= 4096 stages only the Scalars: CTA 0
+    // prefetches the mirror column into L1 instead, because every CTA of the
+    // launch would reserve that buffer, and the shared-memory carve-out it
+    // takes comes out of the L1 that holds the stage inputs prefetched during
+    // Q's transform (4096^2: column pass 131 -> 122 us with the mirror and the
+    // row sums out of shared memory; at 2048 neutral).
     static constexpr bool OWN = !(VAR == 2 && LOGNY >= 12);
-    static constexpr bool PS = XB + SCB + WPB <= LIM;                            // Scalars
-    static constexpr bool PF = OWN && PS && XB + SCB + PFB + WPB <= LIM;         // + row sums
-    static constexpr bool PM = PF && XB + SCB + PFB + MIB + WPB <= LIM;          // + mirror column
-    static constexpr size_t O_SC = XB, O_PF = O_SC + SCB, O_MI = O_PF + (PF ? PFB : 0);
+    static constexpr bool PS = XB + SCB + WPB <= LIM;                   // Scalars
+    static constexpr bool PM = OWN && PS && XB + SCB + MIB + WPB <= LIM;  // + mirror column
+    static constexpr size_t O_SC = XB, O_MI = O_SC + SCB;
     static constexpr size_t O_WP = O_MI + (PM ? MIB : 0);
-    static constexpr int CE = 16 / (int)sizeof(T);                     // row sums per 16-byte copy
+    static constexpr int CE = 16 / (int)sizeof(T);                     // row sums per 16-byte read
 
     static constexpr size_t smem_bytes() { return O_WP + WPB; }
+
+    // CTAs of a launch: the column groups, then one more, the reducer, which
+    // carries no columns (launch sites: grid = ctas(a)).
+    static AF_HD int col_ctas(const StepArgs<T> &a) { return (a.ntp * W + COLS - 1) / COLS; }
+    static AF_HD int ctas(const StepArgs<T> &a) { return col_ctas(a) + 1; }
+
+    // The reducer CTA: the energy and the mean-flow right-hand side from the
+    // row sums (compensated sums, about double accuracy; the reference sums
+    // the energy in float on the host, ActFlow_V3-2.cu:1118-1124), and the
+    // mean-flow scalar update of this stage -- -beta' Re F[|u|^2 u](0)
+    // (ActFlow_V3-2.cu:1086-1087) and its stage updates (ActFlow_V3-2.cu:
+    // 729-732, 756-759, 778-781, 799-802, 820-821).  Its own CTA keeps this
+    // serial work off the column groups' critical path; the next row pass
+    // adds the updated mean velocity m_appr in real space.  It writes only
+    // m_old, m_new, m_appr and the energy (CTA 0 owns step and nan_step).
+    template <class Sync>
+    static AF_HD void reduce_scalars(const StepArgs<T> &a, int tid, unsigned char *smem, Sync &&sync)
+    {
+        RowAcc<T> *wp = reinterpret_cast<RowAcc<T> *>(smem + O_WP);   // warp partials
+        const int ny = a.ny;
+        RowAcc<T> sum[3];
+        if constexpr (MODE != 0) {
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+                for (int q = tid; q < ny / CE; q += THREADS) {
+                    const T *src = a.rowp + (size_t)k * ny + q * CE;
+#pragma unroll
+                    for (int e = 0; e < CE; e++) sum[k].add(src[e]);
+                }
+        }
+        block_sum3(sum, tid, wp, sync);
+        if (tid == 0) {
+            Scalars *g = a.sc;
+            double m_old[2] = {g->m_old[0], g->m_old[1]}, m_new[2] = {g->m_new[0], g->m_new[1]};
+            double m_appr[2] = {g->m_appr[0], g->m_appr[1]};
+            const double red[3] = {sum[0].value(), sum[1].value(), sum[2].value()};
+            // (the dt factors come precomputed from the host: no FP64
+            // division on this serial path)
+            const double n0 = -a.beta_sd * red[1], n1 = -a.beta_sd * red[2];
+            const double dd = (double)a.dt;
+            if constexpr (MODE == 0) {
+                for (int d = 0; d < 2; d++) m_old[d] = m_appr[d] = m_new[d];
+            } else if constexpr (MODE == 1) {
+                a.energy[g->step % a.ecap] = red[0] * a.inv_2n3;
+                m_new[0] += a.mf_d6l * n0;
+                m_new[1] += a.mf_d6l * n1;
+                m_appr[0] = a.lin2_v * (m_old[0] + a.mf_d2 * n0);
+                m_appr[1] = a.lin2_v * (m_old[1] + a.mf_d2 * n1);
+            } else if constexpr (MODE == 2) {
+                m_new[0] += a.mf_d3l2 * n0;
+                m_new[1] += a.mf_d3l2 * n1;
+                m_appr[0] = a.lin2_v * (m_old[0] + a.mf_d2 * n0);
+                m_appr[1] = a.lin2_v * (m_old[1] + a.mf_d2 * n1);
+            } else if constexpr (MODE == 3) {
+                m_new[0] += a.mf_d3l2 * n0;
+                m_new[1] += a.mf_d3l2 * n1;
+                m_appr[0] = a.lin_v * (m_old[0] + dd * n0);
+                m_appr[1] = a.lin_v * (m_old[1] + dd * n1);
+            } else {
+                m_new[0] += a.mf_d6 * n0;
+                m_new[1] += a.mf_d6 * n1;
+                for (int d = 0; d < 2; d++) m_old[d] = m_appr[d] = m_new[d];
+            }
+            for (int d = 0; d < 2; d++) {
+                g->m_old[d] = m_old[d];
+                g->m_new[d] = m_new[d];
+                g->m_appr[d] = m_appr[d];
+            }
+        }
+    }
 
     template <class Sync>
     static AF_HD void body(const StepArgs<T> &a, int tid, int bid, unsigned char *smem, Sync &&sync)
     {
+        if (bid == col_ctas(a)) {   // the reducer (uniform over the CTA)
+            reduce_scalars(a, tid, smem, sync);
+            return;
+        }
         const int tl = tid / (CW * TPC);
         const int rem = tid % (CW * TPC);
         const int c = rem % CW, j = rem / CW;
@@ -1184,8 +1275,6 @@ struct ColPass {
         Buf buf{reinterpret_cast<cpx<T> *>(smem) + (size_t)tl * BUFS};
         const Scalars *ssm = reinterpret_cast<const Scalars *>(smem + O_SC);   // owner copies
         cpx<T> *mir = reinterpret_cast<cpx<T> *>(smem + O_MI);
-        T *rsm = reinterpret_cast<T *>(smem + O_PF);
-        RowAcc<T> *wp = reinterpret_cast<RowAcc<T> *>(smem + O_WP);   // warp partials
         const bool owner = bid == 0;   // this CTA holds column kx = 0
         const T kxv = active ? a.kxt[kx] : (T)0;
         const size_t cbase = active ? (size_t)tile * ny * W + kx % W : 0;
@@ -1197,10 +1286,9 @@ struct ColPass {
         const cpx<T> *hin = a.hcol + (size_t)(MODE & 1) * ny;
         cpx<T> *hout = a.hcol + (size_t)((MODE + 1) & 1) * ny;
 
-        // The owner fetches its extra inputs now.  The row sums are summed by
-        // the threads that copied them; the Scalars are read by thread 0, which
-        // copied them; the mirror column is read by other threads after the
-        // barrier at the start of the second forward transform.
+        // The owner fetches its extra inputs now.  The Scalars (their step
+        // counters) are read by thread 0 and the mirror column by the kx = 0
+        // column's threads, both after the barriers of the forward transforms.
         if constexpr (MODE != 0 && PS) {
             if (owner) {
                 if (tid < 4) cp_async16(smem + O_SC + 16 * tid, reinterpret_cast<const unsigned char *>(a.sc) + 16 * tid);
@@ -1213,17 +1301,7 @@ struct ColPass {
                     constexpr int CC = 16 / (int)sizeof(cpx<T>);
                     for (int q = tid; q < ny / CC; q += THREADS) cp_async16(mir + q * CC, hin + q * CC);
                 }
-                if constexpr (PF) {
-#pragma unroll
-                    for (int k = 0; k < 3; k++)
-                        for (int q = tid; q < ny / CE; q += THREADS)
-                            cp_async16(rsm + (size_t)k * ny + q * CE, a.rowp + (size_t)k * ny + q * CE);
-                }
                 cp_async_commit();
-                if constexpr (!PF) {   // the row sums, 128-byte lines
-                    constexpr int PL = 128 / (int)sizeof(T);
-                    for (int q = tid; q < 3 * ny / PL; q += THREADS) prefetch_l1(a.rowp + (size_t)q * PL);
-                }
                 if constexpr (!PM) {   // the mirror source: four tile rows per line (MODE 1), or hin
                     if constexpr (MODE == 1) {
                         for (int q = tid; q < ny / 4; q += THREADS) prefetch_l1(a.u0 + (size_t)(4 * q) * W);
@@ -1307,64 +1385,14 @@ struct ColPass {
             }
         }
 
-        // ---- mean flow and energy: reduce the row sums (CTA holding kx = 0)
-        T m0 = 0, m1 = 0;          // mean velocity for the k = 0 slot (thread 0 of the owner)
-        int sc_step = 0, sc_nan = 0;   // step counters (thread 0 of the owner)
-        if (owner) {
-            RowAcc<T> sum[3];
-            if constexpr (MODE != 0) {
-#pragma unroll
-                for (int k = 0; k < 3; k++)
-                    for (int q = tid; q < ny / CE; q += THREADS) {
-                        const T *src = (PF ? rsm : a.rowp) + (size_t)k * ny + q * CE;
-#pragma unroll
-                        for (int e = 0; e < CE; e++) sum[k].add(src[e]);
-                    }
-            }
-            block_sum3(sum, tid, wp, sync);
-            if (tid == 0) {
-                Scalars s = (MODE != 0 && PS) ? *ssm : *a.sc;
-                const double red[3] = {sum[0].value(), sum[1].value(), sum[2].value()};
-                // Mean-flow right-hand side -beta' Re F[|u|^2 u](0)
-                // (ActFlow_V3-2.cu:1086-1087) and its stage updates
-                // (ActFlow_V3-2.cu:729-732, 756-759, 778-781, 799-802, 820-821).
-                // (the dt factors come precomputed from the host: no FP64
-                // division on this serial path)
-                const double n0 = -a.beta_sd * red[1], n1 = -a.beta_sd * red[2];
-                const double dd = (double)dt;
-                if constexpr (MODE == 0) {
-                    for (int d = 0; d < 2; d++) s.m_old[d] = s.m_appr[d] = s.m_new[d];
-                } else if constexpr (MODE == 1) {
-                    a.energy[s.step % a.ecap] = red[0] * a.inv_2n3;
-                    s.m_new[0] += a.mf_d6l * n0;
-                    s.m_new[1] += a.mf_d6l * n1;
-                    s.m_appr[0] = a.lin2_v * (s.m_old[0] + a.mf_d2 * n0);
-                    s.m_appr[1] = a.lin2_v * (s.m_old[1] + a.mf_d2 * n1);
-                } else if constexpr (MODE == 2) {
-                    s.m_new[0] += a.mf_d3l2 * n0;
-                    s.m_new[1] += a.mf_d3l2 * n1;
-                    s.m_appr[0] = a.lin2_v * (s.m_old[0] + a.mf_d2 * n0);
-                    s.m_appr[1] = a.lin2_v * (s.m_old[1] + a.mf_d2 * n1);
-                } else if constexpr (MODE == 3) {
-                    s.m_new[0] += a.mf_d3l2 * n0;
-                    s.m_new[1] += a.mf_d3l2 * n1;
-                    s.m_appr[0] = a.lin_v * (s.m_old[0] + dd * n0);
-                    s.m_appr[1] = a.lin_v * (s.m_old[1] + dd * n1);
-                } else {
-                    s.m_new[0] += a.mf_d6 * n0;
-                    s.m_new[1] += a.mf_d6 * n1;
-                    for (int d = 0; d < 2; d++) s.m_old[d] = s.m_appr[d] = s.m_new[d];
-                }
-                Scalars *g = a.sc;
-                for (int d = 0; d < 2; d++) {
-                    g->m_old[d] = s.m_old[d];
-                    g->m_new[d] = s.m_new[d];
-                    g->m_appr[d] = s.m_appr[d];
-                }
-                m0 = (T)s.m_appr[0];
-                m1 = (T)s.m_appr[1];
-                sc_step = s.step;
-                sc_nan = s.nan_step;
+        // ---- step counters for the NaN probe (thread 0 of the owner, stage 4;
+        // the reducer CTA updates the mean-flow scalars and the energy)
+        int sc_step = 0, sc_nan = 0;
+        if constexpr (MODE == 4) {
+            if (owner && tid == 0) {
+                const Scalars *sv = PS ? ssm : a.sc;
+                sc_step = sv->step;
+                sc_nan = sv->nan_step;
             }
         }
 
@@ -1430,9 +1458,10 @@ struct ColPass {
             }
         }
 
-        // ---- Biot-Savart (nonl_subfunc_0, ActFlow_V3-2.cu:1176-1180) and the
-        // mean velocity in the k = 0 slot (ActFlow_V3-2.cu:1053-1054), then the
-        // inverse FFT along y of a, ux, uy.
+        // ---- Biot-Savart (nonl_subfunc_0, ActFlow_V3-2.cu:1176-1180), then the
+        // inverse FFT along y of a, ux, uy.  The k = 0 slot of ux, uy (the mean
+        // velocity, ActFlow_V3-2.cu:1053-1054) stays zero here: the next row
+        // pass adds the mean to every real-space value instead.
 #pragma unroll 1
         for (int f = 0; f < 3; f++) {
             cpx<T> v[R];
@@ -1449,8 +1478,7 @@ struct ColPass {
                     cpx<T> u;
                     if constexpr (std::is_same_v<T, df>) u = scale(mk(-w.y, w.x), q);   // packed pipe
                     else u = mk(-w.y * q, w.x * q);
-                    v[r] = (col && (kx != 0 || iy != 0)) ? u : mk<T>(0, 0);
-                    if (owner && kx == 0 && iy == 0) v[r] = mk(f == 1 ? m0 : m1, (T)0);
+                    v[r] = (col && (kx != 0 || iy != 0)) ? u : mk<T>(0, 0);   // k = 0: the mean, added by the row pass
                 }
             }
             fft1<FFTi>(v, j, c, buf, a.twy, 1, sync);

@@ -82,7 +82,7 @@ struct Runner {
                 constexpr int MODE = decltype(tag)::value;
                 auto launch_var = [&](auto vtag) {
                     using CP = ColPass<T, LY, MODE, decltype(vtag)::value>;
-                    launch((a.ntp * Tile<T>::W + CP::COLS - 1) / CP::COLS, CP::THREADS, CP::smem_bytes(),
+                    launch(CP::ctas(a), CP::THREADS, CP::smem_bytes(),
                            [&](int tid, int bid, unsigned char *sm, auto &sync) { CP::body(a, tid, bid, sm, sync); });
                 };
                 // the default shape of the length, and the radix-8 shape at the

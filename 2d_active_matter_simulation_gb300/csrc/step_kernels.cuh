@@ -275,28 +275,11 @@ struct RowPass {
     static constexpr size_t smem_bytes() { return (size_t)ROWS * NBUF * BUFS * sizeof(cpx<T>); }
 
     // C2R pre-processing of X(k), X(M-k): Z(k) = E + i O with
-    // E = X(k) + conj X(M-k), O = (X(k) - conj X(M-k)) exp(2 pi i k / Nx).
-    // A row's element kx lives at row_base + (kx / W) * Ny * W + kx % W.  For
-    // k = j + r TPC with TPC a multiple of W this is a per-thread base plus
-    // r * TPC * Ny: one index computation per transform.
-    static AF_HD cpx<T> pack(const cpx<T> *src, int k, int y, int ny, int kxp, const cpx<T> *twx)
-    {
-        // entries above kxp are zero by construction (pruned transforms) and are not read
-        cpx<T> A = k <= kxp ? src[tidx<T>(k, y, ny)] : mk<T>(0, 0);
-        cpx<T> B = M - k <= kxp ? src[tidx<T>(M - k, y, ny)] : mk<T>(0, 0);
-        return pack_vals(A, B, k, twx);
-    }
-    static AF_HD cpx<T> pack_vals(cpx<T> A, cpx<T> B, int k, const cpx<T> *twx)
-    {
-        if (k == 0) {   // X(0), X(M): imaginary parts dropped, as a half-plane C2R does
-            A.y = 0;
-            B.y = 0;
-        }
-        B.y = -B.y;
-        cpx<T> E = A + B;
-        cpx<T> O = cmulc(A - B, ldtw(twx, k));
-        return mk(E.x - O.y, E.y + O.x);
-    }
+    // E = X(k) + conj X(M-k), O = (X(k) - conj X(M-k)) exp(2 pi i k / Nx)
+    // (load_pairs, then pack_pairs).  A row's element kx lives at
+    // row_base + (kx / W) * Ny * W + kx % W; for k = j + r TPC with TPC a
+    // multiple of W that is a per-thread base plus r * TPC * Ny: one index
+    // computation per transform.
 
     // X(k) and X(M - k) for k = j + r TPC (zero above kxp, not read).
     static AF_HD void load_pairs(cpx<T> (&A)[R], cpx<T> (&B)[R], const cpx<T> *src, int j, int y, int ny, int kxp)
@@ -348,28 +331,6 @@ struct RowPass {
         const cpx<T> E = scale(A + B, (T)0.5);
         const cpx<T> D = scale(A - B, (T)0.5);
         return E + rot<r, 2 * R, -1>(cmul(mk(D.y, -D.x), wj));
-    }
-
-    static AF_HD void load_pack(cpx<T> (&v)[R], const cpx<T> *src, int j, int y, int ny, int kxp,
-                                const cpx<T> *twx)
-    {
-        constexpr int W = Tile<T>::W;
-        if constexpr (TPC % W == 0) {
-            // k = j + r TPC and M - k = (M - j) - r TPC share one base index each
-            const cpx<T> *pa = src + tidx<T>(j, y, ny);
-            const cpx<T> *pb = src + tidx<T>(M - j, y, ny);
-            const size_t stride = (size_t)(TPC / W) * ny * W;
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-                const int k = j + r * TPC;
-                cpx<T> A = k <= kxp ? pa[r * stride] : mk<T>(0, 0);
-                cpx<T> B = M - k <= kxp ? pb[-(long long)(r * stride)] : mk<T>(0, 0);
-                v[r] = pack_vals(A, B, k, twx);
-            }
-        } else {
-#pragma unroll
-            for (int r = 0; r < R; r++) v[r] = pack(src, j + r * TPC, y, ny, kxp, twx);
-        }
     }
 
     // Sum (t0, t1, t2) over the TPC threads of a row in T; the result is valid
